@@ -1,0 +1,469 @@
+"""Benchmark: rasterize-then-splat forward+backward throughput (Mpix/s).
+
+Workload (default `c5`): a ragged batch of 64 seeded meshes (noisy
+icospheres or triangle soups, 50/50), triangle counts lognormal (median 20k,
+sigma 1.2) clipped to [500, 500k], one camera per mesh on a sphere of radius
+3, square resolutions drawn from {256, 512, 1024}, 3 depth layers, back-face
+culling, RGB vertex colors shaded to RGBA (alpha 1). One step = forward
+render of every image + L2 loss against fixed target images + backward to
+vertex positions and vertex colors.
+
+Reported (one JSON line on rank 0):
+  value      batched path: all images in one launch per kernel, the step
+             captured in a CUDA graph and replayed; inputs resident in HBM.
+  plain      the same work as 64 per-mesh render_triangles calls (the
+             reference's vmap 'sequential_unrolled' structure), eager.
+  e2e        the batched step through the public API with pinned host
+             inputs copied in and loss + gradients copied out every step.
+  roofline   dominant kernel: algorithmic bytes / CUDA-event duration vs the
+             measured HBM copy bandwidth.
+  cpu_baseline  the CPU port of the reference path (C restatement of the
+             reference CPU rasterizer + torch CPU restatement of the JAX
+             interpolate/splat/composite and its autodiff), on a sample.
+
+`--impl reference` times that CPU port alone (the reference's own CPU code
+cannot be built on the GPU host: its sources are not there).
+Multi-GPU: replicas only (each rank renders the full batch independently).
+"""
+import argparse
+import concurrent.futures
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--gpus", type=int, default=1)
+  ap.add_argument("--steps", type=int, default=10)
+  ap.add_argument("--warmup", type=int, default=3)
+  ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+  ap.add_argument("--workload", default="c5", choices=["c5", "c2", "c3", "c1"])
+  ap.add_argument("--num-meshes", type=int, default=64)
+  ap.add_argument("--no-cpu-baseline", action="store_true")
+  ap.add_argument("--no-plain", action="store_true")
+  ap.add_argument("--cpu-budget", type=float, default=20.0,
+                  help="seconds of CPU work per reference-arm step / baseline")
+  return ap.parse_args()
+
+
+# --------------------------------------------------------------- workload
+class Workload:
+  """Seeded meshes, cameras, resolutions and target images."""
+
+  def __init__(self, name, num_meshes, seed=0):
+    from diffren_gb300 import workloads as wl
+    self.name = name
+    if name == "c5":
+      meshes, cams, sizes = wl.ragged_batch(num_meshes, seed=seed)
+      desc = ("ragged batch of %d meshes (icosphere|soup), T lognormal median 20k "
+              "in [500, 500k], square res in {256,512,1024}, L=3, fwd+bwd L2 loss "
+              "wrt vertices and RGB" % num_meshes)
+    elif name == "c2":
+      m = wl.soup_workload(200000, seed=seed)
+      eyes = wl.sphere_eyes(8, seed=seed + 1)
+      meshes = [m] * 8
+      cams = [wl.camera_matrix(e, 512, 512) for e in eyes]
+      sizes = [(512, 512)] * 8
+      desc = "200k-triangle soup, 8 cameras, 512x512, L=3, fwd+bwd"
+    elif name == "c3":
+      m = wl.icosphere_workload(71, seed=seed)
+      eyes = wl.sphere_eyes(8, seed=seed + 1)
+      meshes = [m] * 8
+      cams = [wl.camera_matrix(e, 1024, 1024) for e in eyes]
+      sizes = [(1024, 1024)] * 8
+      desc = "100k-triangle noisy icosphere, 8 cameras, 1024x1024, L=3, fwd+bwd"
+    else:
+      m = wl.icosphere_workload(16, seed=seed)
+      meshes, cams, sizes = [m], [wl.camera_matrix((0, 0, 3.0), 256, 256)], [(256, 256)]
+      desc = "5120-triangle icosphere, 256x256, L=3, fwd+bwd"
+    self.meshes, self.cams, self.sizes, self.desc = meshes, cams, sizes, desc
+    self.num_layers = 3
+    self.pixels = int(sum(w * h for w, h in sizes))
+    self.triangles = int(sum(len(m.triangles) for m in meshes))
+    rng = np.random.default_rng(seed + 99)
+    self.targets = [rng.uniform(0, 1, (h, w, 4)).astype(np.float32) for w, h in sizes]
+    for t in self.targets:
+      t[..., 3] = 1.0
+
+
+def shader(a):
+  import torch
+  rgb = a["rgb"]
+  return torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+  """nvidia-smi sampling during the timed region."""
+  Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+       "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+       "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+  def __init__(self, gpu_index):
+    self.gpu = gpu_index
+    self.proc = None
+    self.lines = []
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+          ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+           "--format=csv,noheader,nounits", "-lms", "200"],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self.thread = threading.Thread(target=self._read, daemon=True)
+      self.thread.start()
+    except (OSError, FileNotFoundError):
+      self.proc = None
+    return self
+
+  def _read(self):
+    for line in self.proc.stdout:
+      self.lines.append(line.strip())
+
+  def __exit__(self, *a):
+    if self.proc is not None:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except subprocess.TimeoutExpired:
+        self.proc.kill()
+
+  def summary(self):
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in self.lines:
+      p = [x.strip() for x in ln.split(",")]
+      if len(p) < 9:
+        continue
+      try:
+        sm.append(float(p[1]))
+        mx.append(float(p[2]))
+      except ValueError:
+        continue
+      for n, v in zip(names, p[5:9]):
+        if v.lower().startswith("active"):
+          reasons.add(n)
+    if not sm:
+      return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- our arm
+def kernel_bytes(wl, batch, ids_z, C=4, K=3):
+  """Algorithmic (compulsory) HBM bytes per launch of each kernel."""
+  L, P = wl.num_layers, wl.pixels
+  T = wl.triangles
+  fg = int(ids_z)  # foreground layer-pixels of the step
+  return {
+      # indices + 3 gathered clip vertices per triangle, ids + z + bary out
+      "raster": T * (12 + 48) + 20 * L * P,
+      # per layer-pixel: ids, z, bary in (20 B) + K floats out
+      "interp_fwd": L * P * (20 + 4 * K),
+      # per layer-pixel: ids, z, bary, color (20 + 4C) in; composited C out
+      "splat_fwd": L * P * (20 + 4 * C) + 4 * C * P,
+      # d_out in; ids, z, bary, color in; d_color out
+      "splat_bwd": 4 * C * P + L * P * (20 + 4 * C) + L * P * 4 * C,
+      # per layer-pixel: ids, z, bary, d_attr in (fg only gather-scatter)
+      "interp_bwd": L * P * (20 + 4 * K),
+      "fg_layer_pixels": fg,
+  }
+
+
+def run_ours(args, rank, world, device):
+  import torch
+  import torch.distributed as dist
+  from diffren_gb300 import batch as batch_lib
+  from diffren_gb300 import kernels, render
+
+  wl = Workload(args.workload, args.num_meshes)
+  r = batch_lib.BatchRenderer([m.triangles for m in wl.meshes],
+                              [len(m.vertices) for m in wl.meshes], wl.sizes,
+                              num_layers=wl.num_layers, device=device)
+  verts_h = torch.from_numpy(np.concatenate([m.vertices for m in wl.meshes])).pin_memory()
+  cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
+  cams_h = torch.from_numpy(np.stack(wl.cams)).pin_memory()
+  target = torch.from_numpy(np.concatenate([t.reshape(-1, 4) for t in wl.targets])).to(device)
+  verts = verts_h.to(device)
+  cols = cols_h.to(device)
+  cams = cams_h.to(device)
+  g_v = torch.empty_like(verts)
+  g_c = torch.empty_like(cols)
+  loss_out = torch.empty((), device=device)
+
+  def step():
+    v = verts.detach().requires_grad_(True)
+    c = cols.detach().requires_grad_(True)
+    out = r.render(v, {"rgb": c}, cams, shader)
+    loss = (out - target).square().sum()
+    gv, gc = torch.autograd.grad(loss, (v, c))
+    g_v.copy_(gv)
+    g_c.copy_(gc)
+    loss_out.copy_(loss.detach())
+
+  # Eager warm-up on a side stream, then capture the step.
+  s = torch.cuda.Stream(device)
+  s.wait_stream(torch.cuda.current_stream(device))
+  with torch.cuda.stream(s):
+    for _ in range(max(args.warmup, 3)):
+      step()
+  torch.cuda.current_stream(device).wait_stream(s)
+  # Launch count of our kernels in one step (eager).
+  kernels.LAUNCHES.reset()
+  step()
+  torch.cuda.synchronize(device)
+  launches_per_step = kernels.LAUNCHES.count
+  graph = torch.cuda.CUDAGraph()
+  with torch.cuda.graph(graph):
+    step()
+  for _ in range(args.warmup):
+    graph.replay()
+  torch.cuda.synchronize(device)
+
+  def timed(fn, k):
+    if world > 1:
+      dist.barrier()
+    torch.cuda.synchronize(device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(k):
+      fn()
+    e1.record()
+    torch.cuda.synchronize(device)
+    ms = e0.elapsed_time(e1) / k
+    if world > 1:
+      t = torch.tensor([ms], device=device)
+      dist.all_reduce(t, op=dist.ReduceOp.MAX)
+      ms = float(t)
+    return ms
+
+  with ClockSampler(device.index) as clocks:
+    ms = timed(graph.replay, args.steps)
+  clock = clocks.summary()
+  loss_val = float(loss_out)
+
+  # e2e: public API with host buffers; H2D inputs and D2H loss + grads.
+  gv_h = torch.empty_like(verts_h).pin_memory()
+  gc_h = torch.empty_like(cols_h).pin_memory()
+  loss_h = torch.empty((), pin_memory=True)
+
+  def e2e_step():
+    verts.copy_(verts_h, non_blocking=True)
+    cols.copy_(cols_h, non_blocking=True)
+    cams.copy_(cams_h, non_blocking=True)
+    graph.replay()
+    gv_h.copy_(g_v, non_blocking=True)
+    gc_h.copy_(g_c, non_blocking=True)
+    loss_h.copy_(loss_out, non_blocking=True)
+
+  e2e_step()
+  ms_e2e = timed(e2e_step, args.steps)
+  h2d = verts_h.numel() * 4 + cols_h.numel() * 4 + cams_h.numel() * 4
+  d2h = gv_h.numel() * 4 + gc_h.numel() * 4 + 4
+
+  # Per-kernel CUDA-event durations on the launching stream (eager step with
+  # events around each op), for the roofline of the dominant kernel.
+  per_kernel = kernels.profile_step(step, args.steps, device)
+  plain = None
+  if not args.no_plain and rank == 0:
+    plain = run_plain(wl, device, args)
+  return dict(wl=wl, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
+              loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
+              plain=plain, renderer=r)
+
+
+def run_plain(wl, device, args):
+  """64 separate per-mesh renders (eager), same loss and gradients."""
+  import torch
+  from diffren_gb300 import render
+  data = []
+  for m, cam, (w, h), t in zip(wl.meshes, wl.cams, wl.sizes, wl.targets):
+    data.append((torch.tensor(m.vertices, device=device),
+                 torch.tensor(m.colors, device=device),
+                 torch.tensor(m.triangles, device=device),
+                 torch.tensor(cam, device=device), w, h,
+                 torch.tensor(t, device=device)))
+
+  def step():
+    for v0, c0, tri, cam, w, h, tgt in data:
+      v = v0.detach().requires_grad_(True)
+      c = c0.detach().requires_grad_(True)
+      out = render.render_triangles(v, {"rgb": c}, tri, cam, w, h, shader,
+                                    num_layers=wl.num_layers)
+      loss = (out - tgt).square().sum()
+      torch.autograd.grad(loss, (v, c))
+
+  for _ in range(2):
+    step()
+  torch.cuda.synchronize(device)
+  k = max(1, min(args.steps, 3))
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record()
+  for _ in range(k):
+    step()
+  e1.record()
+  torch.cuda.synchronize(device)
+  ms = e0.elapsed_time(e1) / k
+  return {"ms_per_step": ms, "value": wl.pixels / ms / 1e3, "steps": k}
+
+
+# -------------------------------------------------------- CPU (reference)
+def cpu_port_sample(wl, budget_s, threads):
+  """Times the CPU port on images of the workload until `budget_s` of work.
+
+  Rasterization: the C restatement of the reference CPU rasterizer (float
+  depth semantics), images spread over `threads` host threads. Interpolate,
+  shade, splat, normalize, composite, L2 loss and the backward: torch CPU
+  float32 restatement of the reference's JAX code and torch autograd.
+  Returns (pixels, seconds, images used).
+  """
+  import torch
+  from oracle import raster, torch_ref
+  torch.set_num_threads(threads)
+  order = list(range(len(wl.meshes)))
+  px = 0
+  used = 0
+  t_total = 0.0
+  for i in order:
+    m, cam, (w, h), tgt = wl.meshes[i], wl.cams[i], wl.sizes[i], wl.targets[i]
+    t0 = time.perf_counter()
+    clip = raster.transform(cam, m.vertices)
+    ids, z, b = raster.rasterize(clip, m.triangles, w, h, wl.num_layers, 1,
+                                 raster.DEPTH_FLOAT)
+    state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
+    tc = torch.tensor(clip, requires_grad=True)
+    tcol = torch.tensor(m.colors, requires_grad=True)
+    ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
+    rgb = torch_ref.interpolate(tcol, ti, tz, tb, tt)
+    shaded = torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+    out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
+    loss = (out - torch.tensor(tgt)).square().sum()
+    torch.autograd.grad(loss, (tc, tcol))
+    t_total += time.perf_counter() - t0
+    px += w * h
+    used += 1
+    if t_total >= budget_s:
+      break
+  return px, t_total, used
+
+
+def run_reference(args):
+  wl = Workload(args.workload, args.num_meshes)
+  threads = os.cpu_count() or 1
+  # Images are processed one after another, each op using all host threads.
+  vals = []
+  sample = None
+  for it in range(args.warmup + args.steps):
+    px, secs, used = cpu_port_sample(wl, args.cpu_budget / max(1, args.steps), threads)
+    if it >= args.warmup:
+      vals.append(px / secs / 1e6)
+      sample = "first %d of %d images (%d px) per step" % (used, len(wl.meshes), px)
+  value = float(np.median(vals))
+  line = {
+      "metric": "RtS fwd+bwd Mpix/s on 1 GB300, batched vs plain, at 1e-5 rel err",
+      "value": value, "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps,
+      "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+      "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+      "impl": "reference",
+      "config": {"workload": wl.desc, "num_images": len(wl.meshes),
+                 "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
+                 "num_layers": wl.num_layers},
+      "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "port",
+                       "sample": sample},
+      "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
+              "d2h_bytes_per_step": 0},
+  }
+  print(json.dumps(line))
+
+
+def measured_peaks():
+  path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+  try:
+    with open(path) as f:
+      d = json.load(f)
+    return float(d["hbm_gbs"]), "measured"
+  except (OSError, KeyError, ValueError):
+    return 6800.0, "fallback"
+
+
+def main():
+  args = parse()
+  rank = int(os.environ.get("RANK", "0"))
+  world = int(os.environ.get("WORLD_SIZE", "1"))
+  local = int(os.environ.get("LOCAL_RANK", "0"))
+  if args.impl == "reference":
+    if rank == 0:
+      run_reference(args)
+    return
+  import torch
+  import torch.distributed as dist
+  device = torch.device("cuda", local)
+  torch.cuda.set_device(device)
+  if world > 1:
+    dist.init_process_group("nccl", device_id=device)
+  res = run_ours(args, rank, world, device)
+  wl = res["wl"]
+  cpu = None
+  if rank == 0 and not args.no_cpu_baseline:
+    threads = os.cpu_count() or 1
+    px, secs, used = cpu_port_sample(wl, args.cpu_budget, threads)
+    cpu = {"value": px / secs / 1e6, "unit": "Mpix/s", "cores": threads, "kind": "port",
+           "sample": "first %d of %d images of the workload (%d px), fwd+bwd, %.1f s"
+                     % (used, len(wl.meshes), px, secs)}
+  if rank != 0:
+    if world > 1:
+      dist.destroy_process_group()
+    return
+  peak, peak_kind = measured_peaks()
+  pk = res["per_kernel"]
+  dom = max((k for k in pk if k in ("raster", "interp_fwd", "splat_fwd", "splat_bwd",
+                                    "interp_bwd")), key=lambda k: pk[k])
+  nbytes = kernel_bytes(wl, res["renderer"].batch, 0)
+  achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
+  value = world * wl.pixels / res["ms"] / 1e3
+  line = {
+      "metric": "RtS fwd+bwd Mpix/s on 1 GB300, batched vs plain, at 1e-5 rel err",
+      "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+      "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
+      "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (seeded meshes, cameras and targets)",
+      "config": {"workload": wl.desc, "num_images": len(wl.meshes),
+                 "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
+                 "num_layers": wl.num_layers, "parallelism": "replicas" if world > 1 else "1 GPU",
+                 "l2": "per-step working set of several GB > 129 MB L2",
+                 "cuda_graph": True},
+      "e2e": {"value": world * wl.pixels / res["ms_e2e"] / 1e3, "unit": "Mpix/s",
+              "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
+      "plain": None if res["plain"] is None else {
+          "value": res["plain"]["value"], "unit": "Mpix/s",
+          "ms_per_step": res["plain"]["ms_per_step"],
+          "batched_over_plain": value / world / res["plain"]["value"]},
+      "gpu_launches": res["launches"] * args.steps,
+      "kernels_ms": {k: round(v, 4) for k, v in pk.items()},
+      "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
+                   "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                   "algorithmic_bytes": nbytes[dom], "traffic": None},
+      "cpu_baseline": cpu,
+      "clocks": res["clock"],
+      "loss": res["loss"],
+  }
+  print(json.dumps(line))
+  if world > 1:
+    dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+  main()

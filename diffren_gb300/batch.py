@@ -1,0 +1,147 @@
+"""Ragged batches: many meshes, cameras and resolutions in one launch per
+kernel.
+
+The reference batches with jax.vmap, which lowers the rasterizer to one FFI
+call per image (rasterize_triangles_xla.py:68-75, 'sequential_unrolled') and
+needs equal shapes. ``BatchRenderer`` instead packs a fixed ragged batch
+(per-mesh triangle lists and per-image resolutions) once, keeps its own
+rasterizer workspace, and renders all images with one launch sequence:
+transform, setup + tile binning + the persistent fine rasterizer over the
+batch's (image, tile) queue, interpolation, the user's shader on the packed
+buffers, splat/normalize/composite, and the VJP kernels. Because no call
+allocates outside torch's allocator or synchronizes, a whole forward+backward
+step can be captured in a CUDA graph (``torch.cuda.graph``) and replayed.
+
+The shader is called once on the packed buffers, each attribute viewed as
+[1, N, K] with N = num_layers * total pixels, so it must be a per-pixel
+function (the reference's shaders in diffren/jax/utils/shaders.py are).
+"""
+from typing import Callable, Dict, Sequence
+
+import numpy as np
+import torch
+
+from . import constants
+from . import kernels
+
+
+class BatchRenderer:
+
+  def __init__(self, triangles: Sequence, vertex_counts: Sequence[int],
+               resolutions: Sequence, num_layers: int = 1,
+               face_culling_mode=constants.FaceCullingMode.BACK,
+               depth_semantics=constants.DepthSemantics.CUDA, device=None,
+               tile=(0, 0)):
+    if len(triangles) != len(vertex_counts) or len(triangles) != len(resolutions):
+      raise ValueError("triangles, vertex_counts and resolutions differ in length")
+    self.device = torch.device(device or "cuda")
+    tris = [torch.as_tensor(t).reshape(-1, 3).to(torch.int32) for t in triangles]
+    self.batch = kernels.ImageBatch([r[0] for r in resolutions],
+                                    [r[1] for r in resolutions],
+                                    [int(v) for v in vertex_counts],
+                                    [t.shape[0] for t in tris])
+    self.triangles = torch.cat(tris).to(self.device).contiguous() if tris else \
+        torch.zeros(0, 3, dtype=torch.int32, device=self.device)
+    self.num_layers = int(num_layers)
+    self.face_culling_mode = int(face_culling_mode)
+    self.config = kernels.raster_config(num_layers, face_culling_mode,
+                                        int(depth_semantics), tile)
+    self.workspace = kernels.Workspace(self.device)
+    self.workspace.get(kernels.raster_workspace_bytes(self.batch, self.config))
+
+  @property
+  def num_images(self):
+    return self.batch.n
+
+  @property
+  def total_pixels(self):
+    return self.batch.total_pixels
+
+  def rasterize(self, clip):
+    """(ids, z, bary) packed over the batch, from packed clip vertices."""
+    return kernels.rasterize_packed(clip.detach(), self.triangles, self.batch,
+                                    self.config, workspace=self.workspace)
+
+  def render(self, vertices, attributes: Dict[str, torch.Tensor], cameras,
+             shading_function: Callable, compositing_mode=constants.CompositingMode.SPLAT_OVER,
+             return_accum_buffers=False):
+    """Renders every image; returns packed [total_pixels, C] (see images()).
+
+    vertices [sum V, 3|4] packed per mesh; attributes: dict of [sum V, K];
+    cameras [N, 4, 4] (one per image) or None for clip-space vertices.
+    """
+    if (compositing_mode == constants.CompositingMode.SPLAT_OVER and
+        self.face_culling_mode != constants.FaceCullingMode.BACK):
+      raise ValueError("Backface culling must be enabled when using splatting.")
+    b = self.batch
+    vertices = torch.as_tensor(vertices, device=self.device)
+    if vertices.shape[0] != b.total_vertices:
+      raise ValueError("expected %d packed vertices, got %d" % (b.total_vertices,
+                                                                 vertices.shape[0]))
+    if cameras is None:
+      clip = vertices.float().contiguous()
+    else:
+      clip = kernels.transform(vertices.float().contiguous(),
+                               torch.as_tensor(cameras, device=self.device), b)
+    ids, z, bary = self.rasterize(clip)
+    L = self.num_layers
+    keys = list(attributes.keys())
+    parts = [kernels._f32(attributes[k], self.device) for k in keys]
+    widths = [p.shape[1] for p in parts]
+    cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0]
+    interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
+    split = torch.split(interp, widths, dim=1)
+    shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
+    shaded = shaded.reshape(-1, shaded.shape[-1])
+    if compositing_mode == constants.CompositingMode.SPLAT_OVER:
+      return kernels.splat_packed(clip, shaded, bary, self.triangles, ids, z, b, L,
+                                  return_accum_buffers)
+    fg = (z != 1.0).float()[:, None]
+    shaded = shaded * fg
+    if compositing_mode == constants.CompositingMode.NONE:
+      return shaded
+    # OVER: composite each image's layers (front to back).
+    outs = []
+    for i in range(b.n):
+      lay = b.layered_view(shaded, i, L)
+      out = lay[-1]
+      for l in range(L - 2, -1, -1):
+        out = lay[l] + (1.0 - lay[l, ..., -1:]) * out
+      outs.append(out.reshape(-1, out.shape[-1]))
+    return torch.cat(outs)
+
+  def images(self, packed):
+    """List of [H_i, W_i, C] views of a packed composited result."""
+    return [self.batch.image_view(packed, i) for i in range(self.batch.n)]
+
+  def layers(self, packed):
+    """List of [L, H_i, W_i, C] views of a packed layered result."""
+    return [self.batch.layered_view(packed, i, self.num_layers)
+            for i in range(self.batch.n)]
+
+
+def pack_meshes(vertices: Sequence, attributes: Sequence[Dict]):
+  """Concatenates per-mesh vertex arrays and attribute dicts."""
+  v = torch.cat([torch.as_tensor(x) for x in vertices])
+  keys = attributes[0].keys() if attributes else []
+  a = {k: torch.cat([torch.as_tensor(d[k]) for d in attributes]) for k in keys}
+  return v, a
+
+
+def render_triangles_batch(vertices: Sequence, attributes: Sequence[Dict],
+                           triangles: Sequence, cameras, resolutions: Sequence,
+                           shading_function: Callable, num_layers: int = 1,
+                           face_culling_mode=constants.FaceCullingMode.BACK,
+                           compositing_mode=constants.CompositingMode.SPLAT_OVER,
+                           device=None):
+  """render_triangles for a ragged list of meshes; returns a list of images."""
+  r = BatchRenderer(triangles, [len(v) for v in vertices], resolutions, num_layers,
+                    face_culling_mode, device=device)
+  v, a = pack_meshes(vertices, attributes)
+  cams = None if cameras is None else torch.as_tensor(np.asarray(cameras), dtype=torch.float32)
+  out = r.render(v.to(r.device), {k: x.to(r.device) for k, x in a.items()},
+                 None if cams is None else cams.to(r.device), shading_function,
+                 compositing_mode)
+  if compositing_mode == constants.CompositingMode.NONE:
+    return r.layers(out)
+  return r.images(out)

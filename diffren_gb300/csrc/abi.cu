@@ -1,0 +1,209 @@
+// extern "C" entry points of libdiffren_gb300.so (declared in
+// include/diffren_gb300.h). Each validates its arguments, enqueues kernels on
+// the caller's stream and returns a status; messages go to a thread-local
+// string read by dr_last_error().
+#include <string>
+
+#include "diffren_gb300.h"
+#include "internal.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+int finish(int rc, std::string& err) {
+  if (rc != DR_OK) g_error = err.empty() ? "unknown error" : err;
+  return rc;
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+dr_image_desc single_image(int32_t nv, int32_t nt, int32_t w, int32_t h) {
+  dr_image_desc d;
+  d.width = w;
+  d.height = h;
+  d.num_vertices = nv;
+  d.num_triangles = nt;
+  d.vertex_offset = 0;
+  d.triangle_offset = 0;
+  d.pixel_offset = 0;
+  return d;
+}
+
+dr_raster_config default_config(int32_t L, int32_t cull, int32_t depth_mode) {
+  dr_raster_config c;
+  c.num_layers = L;
+  c.face_culling_mode = cull;
+  c.depth_mode = depth_mode;
+  c.tile_width = 0;
+  c.tile_height = 0;
+  c.large_tiles = 0;
+  return c;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dr_last_error(void) { return g_error.c_str(); }
+
+int32_t dr_abi_version(void) { return 1; }
+
+size_t dr_rasterize_batch_workspace_bytes(const dr_image_desc* images,
+                                          int32_t num_images,
+                                          const dr_raster_config* config) {
+  std::string err;
+  const size_t n = dr::raster_workspace_bytes(images, num_images, config, err);
+  if (n == 0) g_error = err;
+  return n;
+}
+
+int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
+                       const dr_image_desc* images, int32_t num_images,
+                       const dr_raster_config* config, int32_t* triangle_ids,
+                       float* z_buffer, float* barycentrics, void* workspace,
+                       size_t workspace_bytes, void* stream) {
+  std::string err;
+  return finish(dr::raster_launch(vertices, triangles, images, num_images, config,
+                                  triangle_ids, z_buffer, barycentrics, workspace,
+                                  workspace_bytes, as_stream(stream), err),
+                err);
+}
+
+size_t dr_rasterize_triangles_workspace_bytes(int32_t num_triangles,
+                                              int32_t image_width,
+                                              int32_t image_height,
+                                              int32_t num_layers) {
+  const dr_image_desc d = single_image(0, num_triangles, image_width, image_height);
+  const dr_raster_config c = default_config(num_layers, DR_CULL_NONE, DR_DEPTH_DISCRETIZED);
+  return dr_rasterize_batch_workspace_bytes(&d, 1, &c);
+}
+
+int dr_rasterize_triangles(const float* vertices, int32_t num_vertices,
+                           const int32_t* triangles, int32_t num_triangles,
+                           int32_t image_width, int32_t image_height,
+                           int32_t num_layers, int32_t face_culling_mode,
+                           int32_t depth_mode, int32_t* triangle_ids,
+                           float* z_buffer, float* barycentrics,
+                           void* workspace, size_t workspace_bytes,
+                           void* stream) {
+  const dr_image_desc d = single_image(num_vertices, num_triangles, image_width, image_height);
+  const dr_raster_config c = default_config(num_layers, face_culling_mode, depth_mode);
+  return dr_rasterize_batch(vertices, triangles, &d, 1, &c, triangle_ids, z_buffer,
+                            barycentrics, workspace, workspace_bytes, stream);
+}
+
+int dr_read_error_flags(const void* workspace, uint32_t* flags, void* stream) {
+  std::string err;
+  if (!workspace || !flags) {
+    err = "workspace and flags must be non-null";
+    return finish(DR_ERR_INVALID_ARGUMENT, err);
+  }
+  const char* p = static_cast<const char*>(workspace) + dr::kErrorFlagsOffset;
+  if (cudaMemcpyAsync(flags, p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                      as_stream(stream)) != cudaSuccess ||
+      cudaStreamSynchronize(as_stream(stream)) != cudaSuccess) {
+    err = std::string("reading error flags: ") + cudaGetErrorString(cudaGetLastError());
+    return finish(DR_ERR_CUDA, err);
+  }
+  return DR_OK;
+}
+
+int dr_transform_vertices(const float* matrices, const float* vertices, int32_t dim,
+                          const dr_image_desc* images, int32_t num_images,
+                          float* clip_vertices, void* stream) {
+  std::string err;
+  return finish(dr::transform_launch(matrices, vertices, dim, images, num_images,
+                                     clip_vertices, as_stream(stream), err),
+                err);
+}
+
+int dr_transform_vertices_bwd(const float* matrices, const float* d_clip_vertices,
+                              int32_t dim, const dr_image_desc* images,
+                              int32_t num_images, float* d_vertices, void* stream) {
+  std::string err;
+  return finish(dr::transform_bwd_launch(matrices, d_clip_vertices, dim, images,
+                                         num_images, d_vertices, as_stream(stream), err),
+                err);
+}
+
+int dr_interpolate_fwd(const float* attributes, int32_t num_channels,
+                       const int32_t* triangles, const int32_t* triangle_ids,
+                       const float* z_buffer, const float* barycentrics,
+                       const float* background, const dr_image_desc* images,
+                       int32_t num_images, int32_t num_layers, float* out,
+                       void* stream) {
+  std::string err;
+  return finish(dr::interp_fwd_launch(attributes, num_channels, triangles, triangle_ids,
+                                      z_buffer, barycentrics, background, images,
+                                      num_images, num_layers, out, as_stream(stream), err),
+                err);
+}
+
+int dr_interpolate_bwd(const float* d_out, const float* attributes,
+                       int32_t num_channels, const int32_t* triangles,
+                       const int32_t* triangle_ids, const float* z_buffer,
+                       const float* barycentrics, const dr_image_desc* images,
+                       int32_t num_images, int32_t num_layers,
+                       float* d_attributes, float* d_barycentrics,
+                       float* d_background, void* stream) {
+  std::string err;
+  return finish(dr::interp_bwd_launch(d_out, attributes, num_channels, triangles,
+                                      triangle_ids, z_buffer, barycentrics, images,
+                                      num_images, num_layers, d_attributes,
+                                      d_barycentrics, d_background, as_stream(stream), err),
+                err);
+}
+
+int dr_diff_barycentrics_fwd(const float* clip_vertices, const int32_t* triangles,
+                             const int32_t* triangle_ids, const float* z_buffer,
+                             const dr_image_desc* images, int32_t num_images,
+                             int32_t num_layers, float* barycentrics, void* stream) {
+  std::string err;
+  return finish(dr::diffbary_fwd_launch(clip_vertices, triangles, triangle_ids, z_buffer,
+                                        images, num_images, num_layers, barycentrics,
+                                        as_stream(stream), err),
+                err);
+}
+
+int dr_diff_barycentrics_bwd(const float* d_barycentrics, const float* clip_vertices,
+                             const int32_t* triangles, const int32_t* triangle_ids,
+                             const float* z_buffer, const dr_image_desc* images,
+                             int32_t num_images, int32_t num_layers,
+                             float* d_clip_vertices, void* stream) {
+  std::string err;
+  return finish(dr::diffbary_bwd_launch(d_barycentrics, clip_vertices, triangles,
+                                        triangle_ids, z_buffer, images, num_images,
+                                        num_layers, d_clip_vertices, as_stream(stream),
+                                        err),
+                err);
+}
+
+int dr_splat_fwd(const float* clip_vertices, const int32_t* triangles,
+                 const int32_t* triangle_ids, const float* z_buffer,
+                 const float* barycentrics, const float* colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* out, float* accum, float* normalized, void* stream) {
+  std::string err;
+  return finish(dr::splat_fwd_launch(clip_vertices, triangles, triangle_ids, z_buffer,
+                                     barycentrics, colors, num_channels, images,
+                                     num_images, num_layers, out, accum, normalized,
+                                     as_stream(stream), err),
+                err);
+}
+
+int dr_splat_bwd(const float* d_out, const float* clip_vertices,
+                 const int32_t* triangles, const int32_t* triangle_ids,
+                 const float* z_buffer, const float* barycentrics, const float* colors,
+                 int32_t num_channels, const dr_image_desc* images, int32_t num_images,
+                 int32_t num_layers, float* d_colors, float* d_clip_vertices,
+                 float* d_barycentrics, void* stream) {
+  std::string err;
+  return finish(dr::splat_bwd_launch(d_out, clip_vertices, triangles, triangle_ids,
+                                     z_buffer, barycentrics, colors, num_channels, images,
+                                     num_images, num_layers, d_colors, d_clip_vertices,
+                                     d_barycentrics, as_stream(stream), err),
+                err);
+}
+
+}  // extern "C"

@@ -1,0 +1,241 @@
+// Shared device code of the diffren_gb300 kernels: the batch table passed by
+// value in kernel parameters, and the exact triangle arithmetic of diffren's
+// rasterizer written with explicitly rounded intrinsics so that nvcc cannot
+// contract or reorder any float operation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "diffren_gb300.h"
+
+namespace dr {
+
+// Triangles, images and tiles of one launch. Passed by value as a kernel
+// parameter so a launch needs no device-side table and is graph-capturable.
+struct Batch {
+  int32_t n;
+  int32_t num_layers;
+  int64_t tri_start[DR_MAX_BATCH_INLINE + 1];   // prefix of num_triangles
+  int64_t pix_prefix[DR_MAX_BATCH_INLINE + 1];  // prefix of width*height
+  int64_t pix_off[DR_MAX_BATCH_INLINE];         // caller's pixel_offset
+  int32_t tile_start[DR_MAX_BATCH_INLINE + 1];  // prefix of tiles per image
+  int32_t width[DR_MAX_BATCH_INLINE];
+  int32_t height[DR_MAX_BATCH_INLINE];
+  int32_t num_vertices[DR_MAX_BATCH_INLINE];
+  int32_t tiles_x[DR_MAX_BATCH_INLINE];
+  int64_t vertex_offset[DR_MAX_BATCH_INLINE];
+  int64_t triangle_offset[DR_MAX_BATCH_INLINE];
+};
+
+// Largest i in [0, n) with start[i] <= key (start[0] == 0, start ascending).
+template <typename T>
+__device__ __forceinline__ int find_segment(const T* start, int n, T key) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= key) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------ exact math
+// Float-to-integer conversions round toward zero, saturate and map NaN to 0
+// (cvt.rzi); int64-to-float rounds to nearest. The CPU checker implements
+// the same rules explicitly.
+__device__ __forceinline__ long long wmul(long long a, long long b) {
+  return (long long)((unsigned long long)a * (unsigned long long)b);
+}
+__device__ __forceinline__ long long wadd(long long a, long long b) {
+  return (long long)((unsigned long long)a + (unsigned long long)b);
+}
+__device__ __forceinline__ long long wsub(long long a, long long b) {
+  return (long long)((unsigned long long)a - (unsigned long long)b);
+}
+__device__ __forceinline__ long long shl16(long long a) {
+  return (long long)((unsigned long long)a << 16);
+}
+
+// ToFixedPoint (rasterize_utils.h:57-59): 16 fractional bits.
+__device__ __forceinline__ long long to_fixed(float f) {
+  return __float2ll_rz(__fmul_rn(f, 65536.0f));
+}
+
+// AddPoint (rasterize_utils.h:75-84) on the running box {l, r, b, t}.
+__device__ __forceinline__ void box_add_point(float x, float y, float w, int W,
+                                              int H, int& l, int& r, int& b,
+                                              int& t) {
+  const float px = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(__fdiv_rn(x, w), 1.0f)),
+                             __int2float_rn(W));
+  const float py = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(__fdiv_rn(y, w), 1.0f)),
+                             __int2float_rn(H));
+  l = min(W, max(0, __float2int_rz(floorf(fminf(__int2float_rn(l), px)))));
+  r = min(W, max(0, __float2int_rz(ceilf(fmaxf(__int2float_rn(r), px)))));
+  b = min(H, max(0, __float2int_rz(floorf(fminf(__int2float_rn(b), py)))));
+  t = min(H, max(0, __float2int_rz(ceilf(fmaxf(__int2float_rn(t), py)))));
+}
+
+// AddNearPoint (rasterize_utils.h:86-99): where edge p0->p1 meets z/w = -1.
+__device__ __forceinline__ void box_add_near(float4 p0, float4 p1, int W, int H,
+                                             int& l, int& r, int& b, int& t) {
+  const float denom =
+      __fsub_rn(__fadd_rn(__fsub_rn(p0.z, p1.z), p0.w), p1.w);
+  if (denom != 0.0f) {
+    const float s = __fdiv_rn(__fadd_rn(p0.z, p0.w), denom);
+    const float x = __fadd_rn(p0.x, __fmul_rn(s, __fsub_rn(p1.x, p0.x)));
+    const float y = __fadd_rn(p0.y, __fmul_rn(s, __fsub_rn(p1.y, p0.y)));
+    const float w = __fadd_rn(p0.w, __fmul_rn(s, __fsub_rn(p1.w, p0.w)));
+    box_add_point(x, y, w, W, H, l, r, b, t);
+  }
+}
+
+__device__ __forceinline__ bool clip_visible(float4 p) {
+  return p.w > 0.0f && p.z >= -p.w;
+}
+
+// ComputeTriangleBoundingBox (rasterize_utils.h:111-161). box = {l, r, b, t}
+// with l, b inclusive and r, t exclusive.
+__device__ __forceinline__ bool triangle_box(float4 v0, float4 v1, float4 v2,
+                                             int W, int H, int4& box) {
+  int l = W, r = 0, b = H, t = 0;
+  const bool s0 = clip_visible(v0), s1 = clip_visible(v1), s2 = clip_visible(v2);
+  if (s0) {
+    box_add_point(v0.x, v0.y, v0.w, W, H, l, r, b, t);
+    if (!s1) box_add_near(v0, v1, W, H, l, r, b, t);
+    if (!s2) box_add_near(v0, v2, W, H, l, r, b, t);
+  }
+  if (s1) {
+    box_add_point(v1.x, v1.y, v1.w, W, H, l, r, b, t);
+    if (!s2) box_add_near(v1, v2, W, H, l, r, b, t);
+    if (!s0) box_add_near(v1, v0, W, H, l, r, b, t);
+  }
+  if (s2) {
+    box_add_point(v2.x, v2.y, v2.w, W, H, l, r, b, t);
+    if (!s0) box_add_near(v2, v0, W, H, l, r, b, t);
+    if (!s1) box_add_near(v2, v1, W, H, l, r, b, t);
+  }
+  box = make_int4(l, r, b, t);
+  return (r > l) && (t > b);
+}
+
+// ComputeUnnormalizedMatrixInverse (rasterize_utils.h:176-206) of the matrix
+// with columns (x_i, y_i, w_i) in 16.16 fixed point. Row i of m holds the
+// coefficients (a, b, c) of edge function i. For NONE and FRONT the reference
+// scales each int64 entry by a float sign, which rounds it to float
+// precision; that rounding is part of the result.
+__device__ __forceinline__ void edge_matrix(float4 v0, float4 v1, float4 v2,
+                                            int culling, long long m[9]) {
+  const long long x0 = to_fixed(v0.x), x1 = to_fixed(v1.x), x2 = to_fixed(v2.x);
+  const long long y0 = to_fixed(v0.y), y1 = to_fixed(v1.y), y2 = to_fixed(v2.y);
+  const long long w0 = to_fixed(v0.w), w1 = to_fixed(v1.w), w2 = to_fixed(v2.w);
+  m[0] = wsub(wmul(y1, w2), wmul(w1, y2));
+  m[1] = wsub(wmul(x2, w1), wmul(w2, x1));
+  m[2] = wsub(wmul(x1, y2), wmul(y1, x2));
+  m[3] = wsub(wmul(y2, w0), wmul(w2, y0));
+  m[4] = wsub(wmul(x0, w2), wmul(w0, x2));
+  m[5] = wsub(wmul(x2, y0), wmul(y2, x0));
+  m[6] = wsub(wmul(y0, w1), wmul(w0, y1));
+  m[7] = wsub(wmul(x1, w0), wmul(w1, x0));
+  m[8] = wsub(wmul(x0, y1), wmul(y0, x1));
+  if (culling == DR_CULL_NONE || culling == DR_CULL_FRONT) {
+    const long long det_i = wadd(wadd(wmul(x0, m[0]), wmul(x1, m[3])), wmul(x2, m[6]));
+    const float det = __ll2float_rn(det_i);
+    const float sign = culling == DR_CULL_NONE ? copysignf(1.0f, det) : -1.0f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) m[i] = __float2ll_rz(__fmul_rn(__ll2float_rn(m[i]), sign));
+  }
+}
+
+// Fixed-point NDC coordinate of the center of pixel i of n
+// (rasterize_utils.h:225-228).
+__device__ __forceinline__ long long pixel_center_fixed(int i, int n) {
+  const float scale = __fdiv_rn(2.0f, __int2float_rn(n));
+  const float p = __fsub_rn(__fmul_rn(scale, __fadd_rn(__int2float_rn(i), 0.5f)), 1.0f);
+  return to_fixed(p);
+}
+
+// Edge functions at a pixel (rasterize_utils.h:220-238).
+__device__ __forceinline__ void edge_values(const long long m[9], long long px,
+                                            long long py, long long e[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    e[i] = wadd(wadd(wmul(m[3 * i], px), wmul(m[3 * i + 1], py)), shl16(m[3 * i + 2]));
+}
+
+// PixelIsInsideTriangle (rasterize_utils.h:243-248).
+__device__ __forceinline__ bool inside(const long long e[3]) {
+  return (e[0] >= 0 && e[1] >= 0 && e[2] >= 0) && (e[0] > 0 || e[1] > 0 || e[2] > 0);
+}
+
+// Perspective-correct barycentrics (rasterize_triangles_impl.cc:79-82).
+__device__ __forceinline__ void barycentrics_of(const long long e[3], float b[3]) {
+  const float sum = __ll2float_rn(wadd(wadd(e[0], e[1]), e[2]));
+  b[0] = __fdiv_rn(__ll2float_rn(e[0]), sum);
+  b[1] = __fdiv_rn(__ll2float_rn(e[1]), sum);
+  b[2] = __fdiv_rn(__ll2float_rn(e[2]), sum);
+}
+
+// NDC depth of a fragment (rasterize_triangles_impl.cc:87-89).
+__device__ __forceinline__ float fragment_z(const float b[3], float3 vz, float3 vw) {
+  const float cz = __fadd_rn(__fadd_rn(__fmul_rn(b[0], vz.x), __fmul_rn(b[1], vz.y)),
+                             __fmul_rn(b[2], vz.z));
+  const float cw = __fadd_rn(__fadd_rn(__fmul_rn(b[0], vw.x), __fmul_rn(b[1], vw.y)),
+                             __fmul_rn(b[2], vw.z));
+  return __fdiv_rn(cz, cw);
+}
+
+// DiscretizeZ / UndiscretizeZ (rasterize_triangles_impl_cuda.cu.cc:143-159):
+// scale = uint32 max / 2 as an integer, arithmetic in double.
+__device__ __forceinline__ uint32_t discretize_z(float z) {
+  return __double2uint_rz(__dmul_rn(__dadd_rn((double)z, 1.0), 2147483647.0));
+}
+__device__ __forceinline__ float undiscretize_z(uint32_t d) {
+  return __double2float_rn(__dsub_rn(__ddiv_rn((double)d, 2147483647.0), 1.0));
+}
+
+// Order-preserving float -> uint32 map with -0 == +0 (float depth keys).
+__device__ __forceinline__ uint32_t float_order_bits(float z) {
+  if (z == 0.0f) z = 0.0f;
+  const uint32_t u = __float_as_uint(z);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ unsigned long long empty_key(int depth_mode) {
+  return depth_mode == DR_DEPTH_DISCRETIZED
+             ? (unsigned long long)4294967294u << 32  // DiscretizeZ(1.0f)
+             : (unsigned long long)float_order_bits(1.0f) << 32;
+}
+
+// ---------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_inclusive_scan(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T o = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += o;
+  }
+  return v;
+}
+
+// Exclusive scan over a block of NT threads; returns the block total.
+template <int NT>
+__device__ __forceinline__ int block_exclusive_scan(int v, int* smem_warp, int& excl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int inc = warp_inclusive_scan(v);
+  if (lane == 31) smem_warp[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < NT / 32 ? smem_warp[lane] : 0;
+    w = warp_inclusive_scan(w);
+    if (lane < NT / 32) smem_warp[lane] = w;
+  }
+  __syncthreads();
+  const int warp_base = warp ? smem_warp[warp - 1] : 0;
+  const int total = smem_warp[NT / 32 - 1];
+  excl = warp_base + inc - v;
+  __syncthreads();
+  return total;
+}
+
+}  // namespace dr

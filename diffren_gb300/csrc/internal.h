@@ -1,0 +1,109 @@
+// Host-side declarations shared by the diffren_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+namespace dr {
+
+// Fills the by-value batch table for images[0, n) (n <= DR_MAX_BATCH_INLINE)
+// with screen tiles of TW x TH pixels.
+inline bool make_batch(const dr_image_desc* images, int n, int L, int TW, int TH,
+                       Batch& b, std::string& err) {
+  std::memset(&b, 0, sizeof(b));
+  b.n = n;
+  b.num_layers = L;
+  int64_t tris = 0, tiles = 0, pix = 0;
+  for (int i = 0; i < n; ++i) {
+    const dr_image_desc& d = images[i];
+    if (d.width <= 0 || d.height <= 0) {
+      err = "image " + std::to_string(i) + ": width and height must be > 0";
+      return false;
+    }
+    if (d.num_triangles < 0 || d.num_vertices < 0 || d.vertex_offset < 0 ||
+        d.triangle_offset < 0 || d.pixel_offset < 0) {
+      err = "image " + std::to_string(i) + ": negative count or offset";
+      return false;
+    }
+    b.tri_start[i] = tris;
+    b.tile_start[i] = int32_t(tiles);
+    b.pix_prefix[i] = pix;
+    b.pix_off[i] = d.pixel_offset;
+    b.width[i] = d.width;
+    b.height[i] = d.height;
+    b.num_vertices[i] = d.num_vertices;
+    b.vertex_offset[i] = d.vertex_offset;
+    b.triangle_offset[i] = d.triangle_offset;
+    b.tiles_x[i] = (d.width + TW - 1) / TW;
+    tris += d.num_triangles;
+    tiles += int64_t(b.tiles_x[i]) * ((d.height + TH - 1) / TH);
+    pix += int64_t(d.width) * d.height;
+  }
+  b.tri_start[n] = tris;
+  b.tile_start[n] = int32_t(tiles);
+  b.pix_prefix[n] = pix;
+  if (tris >= (int64_t(1) << 31) || tiles >= (int64_t(1) << 31)) {
+    err = "batch too large: triangles and tiles must each be < 2^31";
+    return false;
+  }
+  return true;
+}
+
+inline int launch_status(const char* what, std::string& err) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return DR_OK;
+  err = std::string(what) + ": " + cudaGetErrorString(e);
+  return DR_ERR_CUDA;
+}
+
+// raster.cu
+size_t raster_workspace_bytes(const dr_image_desc* images, int n,
+                              const dr_raster_config* cfg, std::string& err);
+int raster_launch(const float* vertices, const int32_t* triangles,
+                  const dr_image_desc* images, int n, const dr_raster_config* cfg,
+                  int32_t* ids, float* z, float* bary, void* workspace,
+                  size_t ws_bytes, cudaStream_t stream, std::string& err);
+// Byte offset of the device error word inside a raster workspace.
+constexpr size_t kErrorFlagsOffset = 4;
+
+// interp.cu
+int transform_launch(const float* matrices, const float* vertices, int dim,
+                     const dr_image_desc* images, int n, float* clip,
+                     cudaStream_t stream, std::string& err);
+int transform_bwd_launch(const float* matrices, const float* d_clip, int dim,
+                         const dr_image_desc* images, int n, float* d_vertices,
+                         cudaStream_t stream, std::string& err);
+int interp_fwd_launch(const float* attr, int K, const int32_t* tris,
+                      const int32_t* ids, const float* z, const float* bary,
+                      const float* background, const dr_image_desc* images, int n,
+                      int L, float* out, cudaStream_t stream, std::string& err);
+int interp_bwd_launch(const float* d_out, const float* attr, int K,
+                      const int32_t* tris, const int32_t* ids, const float* z,
+                      const float* bary, const dr_image_desc* images, int n, int L,
+                      float* d_attr, float* d_bary, float* d_bg,
+                      cudaStream_t stream, std::string& err);
+int diffbary_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
+                        const float* z, const dr_image_desc* images, int n, int L,
+                        float* bary, cudaStream_t stream, std::string& err);
+int diffbary_bwd_launch(const float* d_bary, const float* clip, const int32_t* tris,
+                        const int32_t* ids, const float* z,
+                        const dr_image_desc* images, int n, int L, float* d_clip,
+                        cudaStream_t stream, std::string& err);
+
+// splat.cu
+int splat_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
+                     const float* z, const float* bary, const float* colors, int C,
+                     const dr_image_desc* images, int n, int L, float* out,
+                     float* accum, float* normalized, cudaStream_t stream,
+                     std::string& err);
+int splat_bwd_launch(const float* d_out, const float* clip, const int32_t* tris,
+                     const int32_t* ids, const float* z, const float* bary,
+                     const float* colors, int C, const dr_image_desc* images, int n,
+                     int L, float* d_colors, float* d_clip, float* d_bary,
+                     cudaStream_t stream, std::string& err);
+
+}  // namespace dr

@@ -1,0 +1,537 @@
+// Multi-layer z-buffer rasterizer for GB300: triangle setup, screen-tile
+// binning and a persistent shared-memory fine rasterizer over an
+// (image, tile) work queue. One launch sequence covers a whole ragged batch.
+//
+// Results are bit-identical to diffren's rasterizers
+// (diffren/common/kernels/rasterize_triangles_impl_cuda.cu.cc:244-395 for
+// DR_DEPTH_DISCRETIZED, rasterize_triangles_impl.cc:27-118 for
+// DR_DEPTH_FLOAT): the per-fragment arithmetic is the reference's, and each
+// pixel keeps the L smallest packed (depth | triangle id) keys, which is
+// independent of the order fragments arrive in.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+#include "internal.h"
+
+static_assert(dr::kErrorFlagsOffset == 4, "error word is counters[1]");
+
+namespace dr {
+namespace {
+
+constexpr int kThreads = 256;  // fine-raster block = triangle chunk size
+constexpr int kDefaultTile = 16;
+constexpr int kDefaultLargeTiles = 16;
+
+struct __align__(16) TriSetup {
+  long long m[9];  // edge-function coefficients (unnormalized inverse)
+  float vz[3];     // clip z of the three vertices
+  float vw[3];     // clip w of the three vertices
+};
+static_assert(sizeof(TriSetup) == 96, "TriSetup layout");
+
+struct RasterArgs {
+  const float4* verts;
+  const int32_t* tris;
+  int culling, depth_mode, L, TW, TH, large_tiles;
+  int64_t total_tris;
+  int32_t total_tiles;
+  TriSetup* setup;
+  int4* bbox;  // {left, right, bottom, top}; empty when culled
+  int32_t* tile_count;
+  int32_t* tile_fill;
+  int32_t* tile_first;  // exclusive scan of tile_count, total_tiles + 1
+  int32_t* bins;        // global triangle indices grouped by tile
+  int32_t* large_count;  // per image
+  int32_t* large_list;   // per image, at tri_start[image]
+  uint32_t* counters;    // [0] work queue head, [1] error flags
+  int32_t* ids;
+  float* z;
+  float* bary;
+};
+
+// Workspace: the zeroed block first, then the rest; 256-byte aligned parts.
+struct Layout {
+  size_t counters, tile_count, tile_fill, large_count, zero_end;
+  size_t tile_first, setup, bbox, bins, large_list, total;
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+Layout make_layout(int64_t tris, int64_t tiles, int images, int large_tiles) {
+  Layout l;
+  size_t o = 0;
+  l.counters = o; o = align_up(o + 64);  // [0] queue head, [1] error flags
+  l.tile_count = o; o = align_up(o + 4 * tiles);
+  l.tile_fill = o; o = align_up(o + 4 * tiles);
+  l.large_count = o; o = align_up(o + 4 * size_t(images));
+  l.zero_end = o;
+  l.tile_first = o; o = align_up(o + 4 * (tiles + 1));
+  l.setup = o; o = align_up(o + sizeof(TriSetup) * tris);
+  l.bbox = o; o = align_up(o + 16 * tris);
+  l.bins = o; o = align_up(o + 4 * size_t(large_tiles) * tris);
+  l.large_list = o; o = align_up(o + 4 * tris);
+  l.total = o;
+  return l;
+}
+
+// True when no pixel center of `box` can pass the inside test: the sum of
+// the three edge functions is linear in the fixed-point pixel coordinates
+// (which are monotone in the pixel index), so it is <= 0 over the whole box
+// iff it is <= 0 at the four corners. Only used when no int64 term can
+// overflow (|m| < 2^43), so the test is exact.
+__device__ bool cannot_cover(const long long m[9], int4 box, int W, int H) {
+  const long long lim = 1LL << 43;
+#pragma unroll
+  for (int i = 0; i < 9; ++i)
+    if (m[i] >= lim || m[i] <= -lim) return false;
+  const long long A = m[0] + m[3] + m[6];
+  const long long B = m[1] + m[4] + m[7];
+  const long long C = (m[2] + m[5] + m[8]) * 65536;
+  const long long x0 = pixel_center_fixed(box.x, W), x1 = pixel_center_fixed(box.y - 1, W);
+  const long long y0 = pixel_center_fixed(box.z, H), y1 = pixel_center_fixed(box.w - 1, H);
+  const long long s00 = A * x0 + B * y0 + C, s10 = A * x1 + B * y0 + C;
+  const long long s01 = A * x0 + B * y1 + C, s11 = A * x1 + B * y1 + C;
+  return s00 <= 0 && s10 <= 0 && s01 <= 0 && s11 <= 0;
+}
+
+__device__ __forceinline__ void tile_rect(int4 box, int TW, int TH, int& tx0,
+                                          int& tx1, int& ty0, int& ty1) {
+  tx0 = box.x / TW;
+  tx1 = (box.y - 1) / TW;
+  ty0 = box.z / TH;
+  ty1 = (box.w - 1) / TH;
+}
+
+// One thread per triangle of the batch: bounding box, edge matrix, exact
+// coverage cull, per-tile counts (small triangles) or the large list.
+__global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
+  const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (g >= a.total_tris) return;
+  const int img = find_segment(B.tri_start, B.n, g);
+  const int64_t t = g - B.tri_start[img];
+  const int W = B.width[img], H = B.height[img];
+  const int32_t* tri = a.tris + 3 * (B.triangle_offset[img] + t);
+  const int i0 = tri[0], i1 = tri[1], i2 = tri[2];
+  const unsigned nv = unsigned(B.num_vertices[img]);
+  int4 box = make_int4(0, 0, 0, 0);
+  bool valid = false;
+  if (unsigned(i0) >= nv || unsigned(i1) >= nv || unsigned(i2) >= nv) {
+    atomicOr(&a.counters[1], DR_FLAG_INDEX_OUT_OF_RANGE);
+  } else {
+    const float4* vb = a.verts + B.vertex_offset[img];
+    const float4 v0 = vb[i0], v1 = vb[i1], v2 = vb[i2];
+    valid = triangle_box(v0, v1, v2, W, H, box);
+    if (valid) {
+      TriSetup s;
+      edge_matrix(v0, v1, v2, a.culling, s.m);
+      valid = !cannot_cover(s.m, box, W, H);
+      if (valid) {
+        s.vz[0] = v0.z; s.vz[1] = v1.z; s.vz[2] = v2.z;
+        s.vw[0] = v0.w; s.vw[1] = v1.w; s.vw[2] = v2.w;
+        const int4* src = reinterpret_cast<const int4*>(&s);
+        int4* dst = reinterpret_cast<int4*>(a.setup + g);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dst[k] = src[k];
+      }
+    }
+  }
+  if (!valid) box = make_int4(0, 0, 0, 0);
+  a.bbox[g] = box;
+  if (!valid) return;
+  int tx0, tx1, ty0, ty1;
+  tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
+  const int n = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+  if (n <= a.large_tiles) {
+    const int base = B.tile_start[img], tx = B.tiles_x[img];
+    for (int y = ty0; y <= ty1; ++y)
+      for (int x = tx0; x <= tx1; ++x) atomicAdd(&a.tile_count[base + y * tx + x], 1);
+  } else {
+    const int slot = atomicAdd(&a.large_count[img], 1);
+    a.large_list[B.tri_start[img] + slot] = int(g);
+  }
+}
+
+// Exclusive scan of the per-tile counts (one block; tiles are few).
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
+                                                         int32_t* first, int n) {
+  __shared__ int warp_sums[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  constexpr int kItems = 4;
+  for (int base = 0; base < n; base += 1024 * kItems) {
+    int v[kItems], s = 0;
+#pragma unroll
+    for (int j = 0; j < kItems; ++j) {
+      const int i = base + threadIdx.x * kItems + j;
+      v[j] = i < n ? count[i] : 0;
+      s += v[j];
+    }
+    int excl;
+    const int total = block_exclusive_scan<1024>(s, warp_sums, excl);
+    int run = carry + excl;
+#pragma unroll
+    for (int j = 0; j < kItems; ++j) {
+      const int i = base + threadIdx.x * kItems + j;
+      if (i < n) first[i] = run;
+      run += v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) first[n] = carry;
+}
+
+// One thread per triangle: writes its index into the bin of every tile its
+// box touches. Order inside a bin is irrelevant to the result.
+__global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B) {
+  const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (g >= a.total_tris) return;
+  const int4 box = a.bbox[g];
+  if (box.y <= box.x) return;
+  int tx0, tx1, ty0, ty1;
+  tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
+  if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > a.large_tiles) return;
+  const int img = find_segment(B.tri_start, B.n, g);
+  const int base = B.tile_start[img], tx = B.tiles_x[img];
+  for (int y = ty0; y <= ty1; ++y)
+    for (int x = tx0; x <= tx1; ++x) {
+      const int tile = base + y * tx + x;
+      const int pos = a.tile_first[tile] + atomicAdd(&a.tile_fill[tile], 1);
+      a.bins[pos] = int(g);
+    }
+}
+
+struct FineSmem {
+  long long* m;          // [9][kThreads]
+  float* vz;             // [3][kThreads]
+  float* vw;             // [3][kThreads]
+  int* tid;              // [kThreads] local triangle id
+  int* geom;             // [kThreads] x0 | y0 << 8 | width << 16 (tile-local)
+  int* off;              // [kThreads] exclusive candidate offsets
+  long long* pxf;        // [TW] fixed-point pixel-center x
+  long long* pyf;        // [TH]
+  unsigned long long* keys;  // [L][TW*TH]
+};
+
+__host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
+  return size_t(9) * kThreads * 8 + size_t(TW + TH) * 8 +
+         size_t(L) * TW * TH * 8 + size_t(6) * kThreads * 4 +
+         size_t(3) * kThreads * 4 + 64;
+}
+
+// Persistent fine rasterizer. Each block takes (image, tile) items from a
+// global queue, keeps the tile's L x TW x TH packed keys in shared memory,
+// and spreads the (triangle, pixel) candidates of each chunk of the tile's
+// triangles evenly over its threads (block prefix scan + binary search), so
+// large and small triangles cost the same per pixel.
+__global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Batch B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_warp[kThreads / 32];
+  __shared__ int s_item;
+  const int TW = a.TW, TH = a.TH, TP = TW * TH, L = a.L;
+  FineSmem s;
+  {
+    unsigned char* p = smem_raw;
+    s.keys = reinterpret_cast<unsigned long long*>(p); p += size_t(L) * TP * 8;
+    s.m = reinterpret_cast<long long*>(p); p += size_t(9) * kThreads * 8;
+    s.pxf = reinterpret_cast<long long*>(p); p += size_t(TW) * 8;
+    s.pyf = reinterpret_cast<long long*>(p); p += size_t(TH) * 8;
+    s.vz = reinterpret_cast<float*>(p); p += size_t(3) * kThreads * 4;
+    s.vw = reinterpret_cast<float*>(p); p += size_t(3) * kThreads * 4;
+    s.tid = reinterpret_cast<int*>(p); p += kThreads * 4;
+    s.geom = reinterpret_cast<int*>(p); p += kThreads * 4;
+    s.off = reinterpret_cast<int*>(p);
+  }
+  const unsigned long long kEmpty = empty_key(a.depth_mode);
+  const bool disc = a.depth_mode == DR_DEPTH_DISCRETIZED;
+
+  for (;;) {
+    if (threadIdx.x == 0) s_item = int(atomicAdd(&a.counters[0], 1u));
+    __syncthreads();
+    const int item = s_item;
+    if (item >= a.total_tiles) break;
+    const int img = find_segment(B.tile_start, B.n, item);
+    const int local = item - B.tile_start[img];
+    const int W = B.width[img], H = B.height[img];
+    const int ntx = B.tiles_x[img];
+    const int x0 = (local % ntx) * TW, y0 = (local / ntx) * TH;
+    const int tw = min(TW, W - x0), th = min(TH, H - y0);
+    const int64_t tri0 = B.tri_start[img];
+
+    for (int p = threadIdx.x; p < L * TP; p += kThreads) s.keys[p] = kEmpty;
+    for (int i = threadIdx.x; i < TW + TH; i += kThreads) {
+      if (i < TW) s.pxf[i] = pixel_center_fixed(x0 + i, W);
+      else s.pyf[i - TW] = pixel_center_fixed(y0 + i - TW, H);
+    }
+    const int nbin = a.tile_count[item];
+    const int bin0 = a.tile_first[item];
+    const int nlarge = a.large_count[img];
+    const int nsrc = nbin + nlarge;
+    __syncthreads();
+
+    for (int c0 = 0; c0 < nsrc; c0 += kThreads) {
+      const int i = c0 + threadIdx.x;
+      int cnt = 0;
+      if (i < nsrc) {
+        const int g = i < nbin ? a.bins[bin0 + i] : a.large_list[tri0 + (i - nbin)];
+        const int4 box = a.bbox[g];
+        const int cx0 = max(box.x, x0) - x0, cx1 = min(box.y, x0 + tw) - x0;
+        const int cy0 = max(box.z, y0) - y0, cy1 = min(box.w, y0 + th) - y0;
+        if (cx1 > cx0 && cy1 > cy0) {
+          cnt = (cx1 - cx0) * (cy1 - cy0);
+          const TriSetup* src = a.setup + g;
+          const int4* q = reinterpret_cast<const int4*>(src);
+          int4 r[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) r[k] = __ldg(q + k);
+          const long long* mm = reinterpret_cast<const long long*>(r);
+          const float* ff = reinterpret_cast<const float*>(r) + 18;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) s.m[k * kThreads + threadIdx.x] = mm[k];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            s.vz[k * kThreads + threadIdx.x] = ff[k];
+            s.vw[k * kThreads + threadIdx.x] = ff[3 + k];
+          }
+          s.tid[threadIdx.x] = int(g - tri0);
+          s.geom[threadIdx.x] = cx0 | (cy0 << 8) | ((cx1 - cx0) << 16);
+        }
+      }
+      int excl;
+      const int total = block_exclusive_scan<kThreads>(cnt, s_warp, excl);
+      s.off[threadIdx.x] = excl;
+      __syncthreads();
+
+      for (int k = threadIdx.x; k < total; k += kThreads) {
+        const int j = find_segment(s.off, kThreads, k);
+        const int geom = s.geom[j];
+        const int w = geom >> 16;
+        const int r = k - s.off[j];
+        const int ry = r / w;
+        const int lx = (geom & 255) + (r - ry * w);
+        const int ly = ((geom >> 8) & 255) + ry;
+        long long m[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = s.m[q * kThreads + j];
+        long long e[3];
+        edge_values(m, s.pxf[lx], s.pyf[ly], e);
+        if (!inside(e)) continue;
+        float b[3];
+        barycentrics_of(e, b);
+        const float3 vz = make_float3(s.vz[j], s.vz[kThreads + j], s.vz[2 * kThreads + j]);
+        const float3 vw = make_float3(s.vw[j], s.vw[kThreads + j], s.vw[2 * kThreads + j]);
+        const float z = fragment_z(b, vz, vw);
+        unsigned long long key;
+        if (disc) {
+          if (z < -1.0f || z > 1.0f) continue;  // NaN passes, as in the reference
+          key = ((unsigned long long)discretize_z(z) << 32) | uint32_t(s.tid[j]);
+        } else {
+          if (!(z >= -1.0f && z < 1.0f)) continue;
+          key = ((unsigned long long)float_order_bits(z) << 32) | uint32_t(s.tid[j]);
+        }
+        if (key >= kEmpty) continue;
+        unsigned long long* kp = s.keys + ly * TW + lx;
+        // Slot values only decrease, so a key above the current last layer
+        // can never be among the pixel's L smallest.
+        if (key > *reinterpret_cast<volatile unsigned long long*>(kp + (L - 1) * TP)) continue;
+        for (int l = 0; l < L; ++l) {
+          const unsigned long long old = atomicMin(kp + l * TP, key);
+          if (old == kEmpty) break;
+          key = max(key, old);
+        }
+      }
+      __syncthreads();
+    }
+
+    // Epilogue: unpack, recompute barycentrics (and float depth) of the
+    // winning triangle at each pixel, write all L layers.
+    const int64_t HW = int64_t(H) * W;
+    const int64_t base = int64_t(L) * B.pix_off[img];
+    for (int p = threadIdx.x; p < TP; p += kThreads) {
+      const int lx = p % TW, ly = p / TW;
+      if (lx >= tw || ly >= th) continue;
+      const int64_t pix = int64_t(y0 + ly) * W + (x0 + lx);
+      for (int l = 0; l < L; ++l) {
+        const unsigned long long key = s.keys[l * TP + p];
+        const int64_t o = base + l * HW + pix;
+        float b[3] = {0.0f, 0.0f, 0.0f};
+        int id;
+        float zz;
+        if (key == kEmpty) {
+          id = disc ? 0 : -1;
+          zz = 1.0f;
+        } else {
+          id = int(uint32_t(key));
+          const TriSetup* st = a.setup + tri0 + id;
+          long long m[9];
+#pragma unroll
+          for (int q = 0; q < 9; ++q) m[q] = __ldg(&st->m[q]);
+          long long e[3];
+          edge_values(m, s.pxf[lx], s.pyf[ly], e);
+          float bb[3];
+          barycentrics_of(e, bb);
+          if (disc) {
+            zz = undiscretize_z(uint32_t(key >> 32));
+          } else {
+            const float3 vz = make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
+            const float3 vw = make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
+            zz = fragment_z(bb, vz, vw);
+          }
+          if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
+        }
+        a.ids[o] = id;
+        a.z[o] = zz;
+        float* bo = a.bary + 3 * o;
+        bo[0] = b[0];
+        bo[1] = b[1];
+        bo[2] = b[2];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int resolve_tile(int v) { return v > 0 ? v : kDefaultTile; }
+
+bool check_config(const dr_raster_config* cfg, int& L, int& TW, int& TH, int& large,
+                  std::string& err) {
+  if (!cfg) { err = "config is null"; return false; }
+  L = cfg->num_layers;
+  TW = resolve_tile(cfg->tile_width);
+  TH = resolve_tile(cfg->tile_height);
+  large = cfg->large_tiles > 0 ? cfg->large_tiles : kDefaultLargeTiles;
+  if (L < 1 || L > DR_MAX_LAYERS) { err = "num_layers must be in [1, 16]"; return false; }
+  if (cfg->face_culling_mode < 0 || cfg->face_culling_mode > 2) {
+    err = "face_culling_mode must be 0, 1 or 2";
+    return false;
+  }
+  if (cfg->depth_mode != DR_DEPTH_DISCRETIZED && cfg->depth_mode != DR_DEPTH_FLOAT) {
+    err = "depth_mode must be 0 (discretized) or 1 (float)";
+    return false;
+  }
+  if (TW > 128 || TH > 128 || TW * TH > 1024) {
+    err = "tile must satisfy width, height <= 128 and width*height <= 1024";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+size_t raster_workspace_bytes(const dr_image_desc* images, int n,
+                              const dr_raster_config* cfg, std::string& err) {
+  int L, TW, TH, large;
+  if (!check_config(cfg, L, TW, TH, large, err)) return 0;
+  if (n < 0 || (n > 0 && !images)) { err = "invalid image table"; return 0; }
+  size_t best = 256;
+  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+    Batch b;
+    if (!make_batch(images + g0, cnt, L, TW, TH, b, err)) return 0;
+    const Layout lay = make_layout(b.tri_start[cnt], b.tile_start[cnt], cnt, large);
+    best = std::max(best, lay.total);
+  }
+  return best;
+}
+
+int raster_launch(const float* vertices, const int32_t* triangles,
+                  const dr_image_desc* images, int n, const dr_raster_config* cfg,
+                  int32_t* ids, float* z, float* bary, void* workspace,
+                  size_t ws_bytes, cudaStream_t stream, std::string& err) {
+  int L, TW, TH, large;
+  if (!check_config(cfg, L, TW, TH, large, err)) return DR_ERR_INVALID_ARGUMENT;
+  if (n < 0 || (n > 0 && !images)) { err = "invalid image table"; return DR_ERR_INVALID_ARGUMENT; }
+  if (n == 0) return DR_OK;
+  if (!ids || !z || !bary || !workspace) {
+    err = "outputs and workspace must be non-null";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  if ((reinterpret_cast<uintptr_t>(vertices) & 15) != 0 ||
+      (reinterpret_cast<uintptr_t>(workspace) & 255) != 0) {
+    err = "vertices must be 16-byte aligned and the workspace 256-byte aligned";
+    return DR_ERR_MISALIGNED;
+  }
+  const size_t smem = fine_smem_bytes(L, TW, TH);
+  static size_t smem_set = 0;
+  if (smem > 48 * 1024 && smem > smem_set) {
+    if (cudaFuncSetAttribute(fine_raster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem)) != cudaSuccess) {
+      err = "tile and layer count need more shared memory than the device has";
+      return DR_ERR_INVALID_ARGUMENT;
+    }
+    smem_set = smem;
+  }
+  // Persistent grid: resident blocks per SM x SMs (cached per smem size).
+  static size_t occ_smem = 0;
+  static int sms = 0, per_sm = 0;
+  if (occ_smem != smem) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fine_raster_kernel, kThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    occ_smem = smem;
+  }
+
+  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+    Batch b;
+    if (!make_batch(images + g0, cnt, L, TW, TH, b, err)) return DR_ERR_INVALID_ARGUMENT;
+    const int64_t tris = b.tri_start[cnt];
+    const int tiles = b.tile_start[cnt];
+    const Layout lay = make_layout(tris, tiles, cnt, large);
+    if (lay.total > ws_bytes) {
+      err = "workspace too small: need " + std::to_string(lay.total) + " bytes";
+      return DR_ERR_WORKSPACE_TOO_SMALL;
+    }
+    char* ws = static_cast<char*>(workspace);
+    RasterArgs a;
+    a.verts = reinterpret_cast<const float4*>(vertices);
+    a.tris = triangles;
+    a.culling = cfg->face_culling_mode;
+    a.depth_mode = cfg->depth_mode;
+    a.L = L; a.TW = TW; a.TH = TH; a.large_tiles = large;
+    a.total_tris = tris;
+    a.total_tiles = tiles;
+    a.setup = reinterpret_cast<TriSetup*>(ws + lay.setup);
+    a.bbox = reinterpret_cast<int4*>(ws + lay.bbox);
+    a.tile_count = reinterpret_cast<int32_t*>(ws + lay.tile_count);
+    a.tile_fill = reinterpret_cast<int32_t*>(ws + lay.tile_fill);
+    a.tile_first = reinterpret_cast<int32_t*>(ws + lay.tile_first);
+    a.bins = reinterpret_cast<int32_t*>(ws + lay.bins);
+    a.large_count = reinterpret_cast<int32_t*>(ws + lay.large_count);
+    a.large_list = reinterpret_cast<int32_t*>(ws + lay.large_list);
+    a.counters = reinterpret_cast<uint32_t*>(ws + lay.counters);
+    a.ids = ids;
+    a.z = z;
+    a.bary = bary;
+
+    if (cudaMemsetAsync(ws, 0, lay.zero_end, stream) != cudaSuccess) {
+      err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(cudaGetLastError());
+      return DR_ERR_CUDA;
+    }
+    if (tris > 0) {
+      const unsigned grid = unsigned((tris + 255) / 256);
+      setup_kernel<<<grid, 256, 0, stream>>>(a, b);
+    }
+    tile_scan_kernel<<<1, 1024, 0, stream>>>(a.tile_count, a.tile_first, tiles);
+    if (tris > 0) {
+      const unsigned grid = unsigned((tris + 255) / 256);
+      bin_scatter_kernel<<<grid, 256, 0, stream>>>(a, b);
+    }
+    const int blocks = std::max(1, std::min(tiles, sms * per_sm));
+    fine_raster_kernel<<<blocks, kThreads, smem, stream>>>(a, b);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      err = std::string("raster launch failed: ") + cudaGetErrorString(e);
+      return DR_ERR_CUDA;
+    }
+  }
+  return DR_OK;
+}
+
+}  // namespace dr

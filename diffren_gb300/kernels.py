@@ -1,0 +1,446 @@
+"""Torch-facing ops over the C ABI: rasterize, transform, interpolate,
+differentiable barycentrics and splat, each with its VJP as an
+``autograd.Function``.
+
+This is the counterpart of diffren/jax/internal/kernels/
+rasterize_triangles_xla.py (the FFI-call layer) extended to every kernel of
+the rasterize-then-splat path. Tensors are device tensors; sizes and the
+current CUDA stream go to the library through ctypes. The ops work on packed
+ragged batches described by an ``ImageBatch``; a single image is a batch of
+one.
+"""
+import contextlib
+import ctypes
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ImageDesc, RasterConfig
+
+
+class _LaunchCounter:
+  """Number of this library's kernels enqueued (per op call)."""
+
+  def __init__(self):
+    self.count = 0
+
+  def reset(self):
+    self.count = 0
+
+
+LAUNCHES = _LaunchCounter()
+_PROFILE = None  # list of (op, start event, end event) while profiling
+
+
+@contextlib.contextmanager
+def _op(name, kernels_launched):
+  LAUNCHES.count += kernels_launched
+  if _PROFILE is None:
+    yield
+    return
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record()
+  yield
+  e1.record()
+  _PROFILE.append((name, e0, e1))
+
+
+def profile_step(step, steps, device):
+  """Mean CUDA-event duration (ms) of each op over `steps` eager calls of
+  `step`; events are recorded on the launching (current) stream."""
+  global _PROFILE
+  totals = {}
+  for _ in range(steps):
+    _PROFILE = []
+    try:
+      step()
+      torch.cuda.synchronize(device)
+      for name, e0, e1 in _PROFILE:
+        totals[name] = totals.get(name, 0.0) + e0.elapsed_time(e1)
+    finally:
+      _PROFILE = None
+  return {k: v / steps for k, v in totals.items()}
+
+
+def _groups(batch):
+  return (batch.n + _lib.DR_MAX_BATCH_INLINE - 1) // _lib.DR_MAX_BATCH_INLINE
+
+
+def _p(t):
+  return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(device=None):
+  return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _f32(t, device=None):
+  t = torch.as_tensor(t, dtype=torch.float32, device=device)
+  return t.contiguous()
+
+
+def _i32(t, device=None):
+  t = torch.as_tensor(t, device=device)
+  return t.to(torch.int32).contiguous()
+
+
+def _require_cuda(*ts):
+  for t in ts:
+    if t is not None and not t.is_cuda:
+      raise ValueError("diffren_gb300 ops take CUDA tensors; got a %s tensor"
+                       % t.device)
+
+
+class ImageBatch:
+  """Host-side table of a batch of images, each with its own mesh.
+
+  Meshes are packed: vertices of image i are rows
+  [vertex_offset[i], vertex_offset[i] + num_vertices[i]) of the packed
+  vertex array, triangles likewise (indices local to the mesh). Layered
+  per-pixel buffers are packed per image as [L, H_i, W_i] blocks, composited
+  images as [H_i, W_i] blocks, in image order.
+  """
+
+  def __init__(self, widths, heights, num_vertices, num_triangles):
+    n = len(widths)
+    if not (len(heights) == len(num_vertices) == len(num_triangles) == n):
+      raise ValueError("per-image lists must have the same length")
+    self.n = n
+    self.widths = [int(w) for w in widths]
+    self.heights = [int(h) for h in heights]
+    self.num_vertices = [int(v) for v in num_vertices]
+    self.num_triangles = [int(t) for t in num_triangles]
+    for w, h in zip(self.widths, self.heights):
+      if w <= 0 or h <= 0:
+        raise ValueError("image width and height must be > 0")
+    self.pixel_offsets = np.concatenate(
+        [[0], np.cumsum([w * h for w, h in zip(self.widths, self.heights)])])
+    self.vertex_offsets = np.concatenate([[0], np.cumsum(self.num_vertices)])
+    self.triangle_offsets = np.concatenate([[0], np.cumsum(self.num_triangles)])
+    self.total_pixels = int(self.pixel_offsets[-1])
+    self.total_vertices = int(self.vertex_offsets[-1])
+    self.total_triangles = int(self.triangle_offsets[-1])
+    self.descs = (ImageDesc * max(n, 1))()
+    for i in range(n):
+      d = self.descs[i]
+      d.width, d.height = self.widths[i], self.heights[i]
+      d.num_vertices, d.num_triangles = self.num_vertices[i], self.num_triangles[i]
+      d.vertex_offset = int(self.vertex_offsets[i])
+      d.triangle_offset = int(self.triangle_offsets[i])
+      d.pixel_offset = int(self.pixel_offsets[i])
+
+  def vertex_image_index(self, device):
+    """[sum V] int64 image index of every packed vertex (cached per device)."""
+    cache = self.__dict__.setdefault("_vidx", {})
+    key = str(device)
+    if key not in cache:
+      idx = np.repeat(np.arange(self.n), self.num_vertices)
+      cache[key] = torch.as_tensor(idx, device=device)
+    return cache[key]
+
+  @classmethod
+  def single(cls, width, height, num_vertices, num_triangles):
+    return cls([width], [height], [num_vertices], [num_triangles])
+
+  @property
+  def ptr(self):
+    return ctypes.cast(self.descs, ctypes.c_void_p)
+
+  def layered_view(self, flat, i, num_layers):
+    """[L, H_i, W_i, ...] view of image i of a packed layered buffer."""
+    h, w = self.heights[i], self.widths[i]
+    a = int(self.pixel_offsets[i]) * num_layers
+    return flat[a:a + num_layers * h * w].view(num_layers, h, w, *flat.shape[1:])
+
+  def image_view(self, flat, i):
+    """[H_i, W_i, ...] view of image i of a packed composited buffer."""
+    h, w = self.heights[i], self.widths[i]
+    a = int(self.pixel_offsets[i])
+    return flat[a:a + h * w].view(h, w, *flat.shape[1:])
+
+
+def raster_config(num_layers, face_culling_mode, depth_mode, tile=(0, 0),
+                  large_tiles=0):
+  c = RasterConfig()
+  c.num_layers = int(num_layers)
+  c.face_culling_mode = int(face_culling_mode)
+  c.depth_mode = int(depth_mode)
+  c.tile_width, c.tile_height = int(tile[0]), int(tile[1])
+  c.large_tiles = int(large_tiles)
+  return c
+
+
+class Workspace:
+  """A growable device scratch buffer for one stream."""
+
+  def __init__(self, device):
+    self.device = device
+    self.buf = None
+
+  def get(self, nbytes):
+    nbytes = max(int(nbytes), 256)
+    if self.buf is None or self.buf.numel() < nbytes:
+      self.buf = torch.empty(nbytes + (nbytes >> 3), dtype=torch.uint8,
+                             device=self.device)
+    return self.buf
+
+
+_ws_lock = threading.Lock()
+_workspaces = {}
+
+
+def default_workspace(device):
+  key = (device.index, torch.cuda.current_stream(device).cuda_stream)
+  with _ws_lock:
+    ws = _workspaces.get(key)
+    if ws is None:
+      ws = _workspaces[key] = Workspace(device)
+  return ws
+
+
+def raster_workspace_bytes(batch, config):
+  lib = _lib.load()
+  n = lib.dr_rasterize_batch_workspace_bytes(batch.ptr, batch.n,
+                                             ctypes.byref(config))
+  if n == 0:
+    raise _lib.DiffrenError(lib.dr_last_error().decode())
+  return n
+
+
+def rasterize_packed(clip, triangles, batch, config, workspace=None, out=None):
+  """Rasterizes a packed batch. Returns flat (ids [L*P], z [L*P], bary [L*P,3]).
+
+  ``clip`` [sum V, 4] float32 and ``triangles`` [sum T, 3] int32 are CUDA
+  tensors; P is the batch's total pixel count.
+  """
+  _require_cuda(clip, triangles)
+  lib = _lib.load()
+  dev = clip.device
+  L = config.num_layers
+  n = L * batch.total_pixels
+  if out is None:
+    ids = torch.empty(n, dtype=torch.int32, device=dev)
+    z = torch.empty(n, dtype=torch.float32, device=dev)
+    bary = torch.empty(n, 3, dtype=torch.float32, device=dev)
+  else:
+    ids, z, bary = out
+  need = raster_workspace_bytes(batch, config)
+  ws = (workspace or default_workspace(dev)).get(need)
+  with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
+    rc = lib.dr_rasterize_batch(_p(clip), _p(triangles), batch.ptr, batch.n,
+                                ctypes.byref(config), _p(ids), _p(z), _p(bary),
+                                _p(ws), ws.numel(), _stream(dev))
+  _lib.check(rc, "dr_rasterize_batch")
+  return ids, z, bary
+
+
+def read_error_flags(workspace, device):
+  lib = _lib.load()
+  flags = ctypes.c_uint32(0)
+  ws = workspace.buf if isinstance(workspace, Workspace) else workspace
+  rc = lib.dr_read_error_flags(_p(ws), ctypes.byref(flags), _stream(device))
+  _lib.check(rc, "dr_read_error_flags")
+  return flags.value
+
+
+# ------------------------------------------------------------- transform
+class _Transform(torch.autograd.Function):
+  """clip = M @ [v, 1] per image (transforms.transform_homogeneous)."""
+
+  @staticmethod
+  def forward(ctx, vertices, matrices, batch):
+    lib = _lib.load()
+    clip = torch.empty(vertices.shape[0], 4, dtype=torch.float32,
+                       device=vertices.device)
+    if vertices.shape[0] > 0:
+      with _op("transform", _groups(batch)):
+        rc = lib.dr_transform_vertices(_p(matrices), _p(vertices),
+                                       int(vertices.shape[1]), batch.ptr, batch.n,
+                                       _p(clip), _stream(vertices.device))
+      _lib.check(rc, "dr_transform_vertices")
+    ctx.save_for_backward(vertices, matrices)
+    ctx.batch = batch
+    return clip
+
+  @staticmethod
+  def backward(ctx, d_clip):
+    vertices, matrices = ctx.saved_tensors
+    batch = ctx.batch
+    dim = vertices.shape[1]
+    d_clip = d_clip.contiguous()
+    d_v = d_m = None
+    # Per image: clip_i = v_h @ M_i^T -> d v_h = d_clip @ M_i, d M_i = d^T v_h.
+    if ctx.needs_input_grad[0]:
+      d_v = torch.empty_like(vertices)
+      with _op("transform_bwd", _groups(batch)):
+        rc = _lib.load().dr_transform_vertices_bwd(_p(matrices), _p(d_clip), dim,
+                                                 batch.ptr, batch.n, _p(d_v),
+                                                 _stream(vertices.device))
+      _lib.check(rc, "dr_transform_vertices_bwd")
+    if ctx.needs_input_grad[1]:
+      idx = batch.vertex_image_index(vertices.device)
+      vh = vertices if dim == 4 else torch.cat(
+          [vertices, torch.ones_like(vertices[:, :1])], dim=1)
+      outer = d_clip[:, :, None] * vh[:, None, :]
+      d_m = torch.zeros_like(matrices).index_add_(0, idx, outer)
+    return d_v, d_m, None
+
+
+def transform(vertices, matrices, batch):
+  """Clip-space vertices [sum V, 4] of a packed batch (one matrix per image)."""
+  vertices = _f32(vertices)
+  matrices = _f32(matrices).reshape(batch.n, 4, 4)
+  _require_cuda(vertices, matrices)
+  if vertices.shape[1] not in (3, 4):
+    raise ValueError("vertices must be [n, 3] or [n, 4]")
+  return _Transform.apply(vertices, matrices, batch)
+
+
+# ---------------------------------------------------------- interpolation
+class _Interpolate(torch.autograd.Function):
+
+  @staticmethod
+  def forward(ctx, attributes, bary, background, triangles, ids, z, batch, L):
+    lib = _lib.load()
+    K = attributes.shape[1]
+    out = torch.empty(ids.shape[0], K, dtype=torch.float32, device=ids.device)
+    with _op("interp_fwd", _groups(batch)):
+      rc = lib.dr_interpolate_fwd(_p(attributes), K, _p(triangles), _p(ids), _p(z),
+                                _p(bary), _p(background), batch.ptr, batch.n, L,
+                                _p(out), _stream(ids.device))
+    _lib.check(rc, "dr_interpolate_fwd")
+    ctx.save_for_backward(attributes, bary, triangles, ids, z)
+    ctx.batch, ctx.L, ctx.has_bg = batch, L, background is not None
+    return out
+
+  @staticmethod
+  def backward(ctx, d_out):
+    attributes, bary, triangles, ids, z = ctx.saved_tensors
+    lib = _lib.load()
+    d_out = d_out.contiguous()
+    d_attr = torch.zeros_like(attributes)
+    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[1] else None
+    d_bg = (torch.zeros(attributes.shape[1], device=attributes.device)
+            if ctx.has_bg and ctx.needs_input_grad[2] else None)
+    with _op("interp_bwd", _groups(ctx.batch)):
+      rc = lib.dr_interpolate_bwd(_p(d_out), _p(attributes), attributes.shape[1],
+                                _p(triangles), _p(ids), _p(z), _p(bary),
+                                ctx.batch.ptr, ctx.batch.n, ctx.L, _p(d_attr),
+                                _p(d_bary), _p(d_bg), _stream(d_out.device))
+    _lib.check(rc, "dr_interpolate_bwd")
+    return d_attr, d_bary, d_bg, None, None, None, None, None
+
+
+def interpolate_packed(attributes, bary, triangles, ids, z, batch, num_layers,
+                       background=None):
+  """Interpolated attributes [L*P, K] of a packed batch."""
+  attributes = _f32(attributes)
+  if attributes.shape[1] > _lib.DR_MAX_CHANNELS:
+    parts = torch.split(attributes, _lib.DR_MAX_CHANNELS, dim=1)
+    bgs = (torch.split(_f32(background, attributes.device), _lib.DR_MAX_CHANNELS)
+           if background is not None else [None] * len(parts))
+    return torch.cat([
+        interpolate_packed(a, bary, triangles, ids, z, batch, num_layers, b)
+        for a, b in zip(parts, bgs)], dim=1)
+  if background is not None:
+    background = _f32(background, attributes.device).reshape(-1)
+  return _Interpolate.apply(attributes, bary, background, triangles, ids, z,
+                            batch, num_layers)
+
+
+# ------------------------------------------- differentiable barycentrics
+class _DiffBary(torch.autograd.Function):
+
+  @staticmethod
+  def forward(ctx, clip, triangles, ids, z, batch, L):
+    lib = _lib.load()
+    bary = torch.empty(ids.shape[0], 3, dtype=torch.float32, device=ids.device)
+    with _op("diffbary_fwd", _groups(batch)):
+      rc = lib.dr_diff_barycentrics_fwd(_p(clip), _p(triangles), _p(ids), _p(z),
+                                      batch.ptr, batch.n, L, _p(bary),
+                                      _stream(ids.device))
+    _lib.check(rc, "dr_diff_barycentrics_fwd")
+    ctx.save_for_backward(clip, triangles, ids, z)
+    ctx.batch, ctx.L = batch, L
+    return bary
+
+  @staticmethod
+  def backward(ctx, d_bary):
+    clip, triangles, ids, z = ctx.saved_tensors
+    lib = _lib.load()
+    d_clip = torch.zeros_like(clip)
+    with _op("diffbary_bwd", _groups(ctx.batch)):
+      rc = lib.dr_diff_barycentrics_bwd(_p(d_bary.contiguous()), _p(clip),
+                                      _p(triangles), _p(ids), _p(z), ctx.batch.ptr,
+                                      ctx.batch.n, ctx.L, _p(d_clip),
+                                      _stream(clip.device))
+    _lib.check(rc, "dr_diff_barycentrics_bwd")
+    return d_clip, None, None, None, None, None
+
+
+def diff_barycentrics_packed(clip, triangles, ids, z, batch, num_layers):
+  return _DiffBary.apply(clip, triangles, ids, z, batch, num_layers)
+
+
+# ------------------------------------------------------------------ splat
+class _Splat(torch.autograd.Function):
+
+  @staticmethod
+  def forward(ctx, clip, colors, bary, triangles, ids, z, batch, L, want_accum):
+    lib = _lib.load()
+    C = colors.shape[1]
+    dev = colors.device
+    out = torch.empty(batch.total_pixels, C, dtype=torch.float32, device=dev)
+    accum = norm = None
+    if want_accum:
+      accum = torch.empty(3 * batch.total_pixels, C, dtype=torch.float32, device=dev)
+      norm = torch.empty_like(accum)
+    with _op("splat_fwd", _groups(batch)):
+      rc = lib.dr_splat_fwd(_p(clip), _p(triangles), _p(ids), _p(z), _p(bary),
+                          _p(colors), C, batch.ptr, batch.n, L, _p(out), _p(accum),
+                          _p(norm), _stream(dev))
+    _lib.check(rc, "dr_splat_fwd")
+    ctx.save_for_backward(clip, colors, bary, triangles, ids, z)
+    ctx.batch, ctx.L = batch, L
+    if want_accum:
+      ctx.mark_non_differentiable(accum, norm)
+      return out, accum, norm
+    return out
+
+  @staticmethod
+  def backward(ctx, d_out, *unused):
+    clip, colors, bary, triangles, ids, z = ctx.saved_tensors
+    lib = _lib.load()
+    d_out = d_out.contiguous()
+    d_colors = torch.empty_like(colors)
+    d_clip = torch.zeros_like(clip)
+    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[2] else None
+    with _op("splat_bwd", _groups(ctx.batch)):
+      rc = lib.dr_splat_bwd(_p(d_out), _p(clip), _p(triangles), _p(ids), _p(z),
+                          _p(bary), _p(colors), colors.shape[1], ctx.batch.ptr,
+                          ctx.batch.n, ctx.L, _p(d_colors), _p(d_clip), _p(d_bary),
+                          _stream(d_out.device))
+    _lib.check(rc, "dr_splat_bwd")
+    return (d_clip if ctx.needs_input_grad[0] else None, d_colors, d_bary, None,
+            None, None, None, None, None)
+
+
+def splat_packed(clip, colors, bary, triangles, ids, z, batch, num_layers,
+                 return_accum_buffers=False):
+  """Splatted, normalized, composited images [P, C] of a packed batch.
+
+  With ``return_accum_buffers`` also returns the accumulated and normalized
+  fg/surface/bg layers, packed [3, H_i, W_i, C] per image (not
+  differentiable).
+  """
+  colors = colors.contiguous()
+  if colors.dtype != torch.float32:
+    colors = colors.float()
+  if colors.shape[1] > _lib.DR_MAX_SPLAT_CHANNELS:
+    raise ValueError("splatting supports at most %d channels" %
+                     _lib.DR_MAX_SPLAT_CHANNELS)
+  return _Splat.apply(clip, colors, bary, triangles, ids, z, batch, num_layers,
+                      bool(return_accum_buffers))

@@ -1,0 +1,80 @@
+"""Main entry point (diffren/jax/render.py:28-140).
+
+``render_triangles`` keeps the reference's signature and behaviour:
+rasterize, interpolate the attribute dict, run the user's deferred shader
+(any differentiable torch function of a dict of [H, W, K] buffers) on each
+layer, then splat+composite (SPLAT_OVER), composite (OVER) or return the
+layers (NONE). Gradients reach vertices, attributes and camera through the
+CUDA VJP kernels; the shader's own VJP is torch autograd.
+
+A leading batch dimension on vertices / camera (/ attributes / triangles)
+renders all images in one launch per kernel, the batched counterpart of
+jax.vmap(render_triangles).
+"""
+from typing import Callable, Dict
+
+import torch
+
+from . import composite
+from . import constants
+from . import interpolate
+from . import rasterize
+from . import splat
+
+
+def _shade_layers(shading_function, interpolated, num_layers, batched):
+  """vmap(shading_function) over layers (and images), as render.py:128."""
+  outs = []
+  if batched:
+    B = next(iter(interpolated.values())).shape[0]
+    for b in range(B):
+      outs.append(torch.stack([
+          shading_function({k: v[b, l] for k, v in interpolated.items()})
+          for l in range(num_layers)]))
+    return torch.stack(outs)
+  return torch.stack([
+      shading_function({k: v[l] for k, v in interpolated.items()})
+      for l in range(num_layers)])
+
+
+def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
+                     camera_matrices, image_width: int, image_height: int,
+                     shading_function: Callable[[Dict[str, torch.Tensor]],
+                                                torch.Tensor],
+                     num_layers: int = 1,
+                     face_culling_mode=constants.FaceCullingMode.BACK,
+                     compositing_mode=constants.CompositingMode.SPLAT_OVER,
+                     return_accum_buffers=False, compute_diff_barys=False,
+                     depth_semantics=constants.DepthSemantics.CUDA):
+  """Rendering with differentiable occlusion using rasterize-then-splat.
+
+  Returns [H, W, C] ([num_layers, H, W, C] for CompositingMode.NONE), with a
+  leading batch dimension when the inputs are batched.
+
+  Raises:
+    ValueError: if face_culling_mode is not BACK and compositing_mode is
+      SPLAT_OVER (back faces would count as occluding layers).
+  """
+  if (compositing_mode == constants.CompositingMode.SPLAT_OVER and
+      face_culling_mode != constants.FaceCullingMode.BACK):
+    raise ValueError("Backface culling must be enabled when using splatting.")
+  vertices = torch.as_tensor(vertices)
+  triangles = torch.as_tensor(triangles)
+  camera = None if camera_matrices is None else torch.as_tensor(camera_matrices)
+  rasterize._validate(vertices, triangles, camera, image_width, image_height,
+                      num_layers)
+  geom = rasterize.Geometry(vertices, triangles, camera, image_width, image_height)
+  frame, _ = rasterize.rasterize_geometry(geom, num_layers, face_culling_mode,
+                                          depth_semantics, compute_diff_barys)
+  interpolated = interpolate.interpolate_vertex_attributes(attributes, frame)
+  shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
+
+  if compositing_mode == constants.CompositingMode.SPLAT_OVER:
+    return splat.splat_clip(geom.clip, frame, shaded, return_accum_buffers)
+
+  shaded = shaded * frame.foreground_mask
+  if compositing_mode == constants.CompositingMode.OVER:
+    if geom.batched:
+      return torch.stack([composite.over(s) for s in shaded])
+    return composite.over(shaded)
+  return shaded

@@ -1,0 +1,225 @@
+/*
+ * diffren_gb300: C ABI of the GB300 (sm_103a) rasterize-then-splat path.
+ *
+ * Every entry point takes device pointers, plain sizes and a cudaStream_t
+ * passed as `void* stream`, enqueues its kernels on that stream and returns
+ * a status code (DR_OK = 0) without synchronizing. No entry point allocates
+ * device memory: scratch space is a caller-owned workspace sized by the
+ * matching *_workspace_bytes function, so every call can be captured in a
+ * CUDA graph. On failure dr_last_error() returns a message (thread-local).
+ *
+ * Layouts (all row-major, float32 / int32):
+ *   vertices      [V, 4]  clip-space xyzw, 16-byte aligned
+ *   triangles     [T, 3]  vertex indices local to their mesh
+ *   triangle_ids  [L, H, W], z_buffer [L, H, W], barycentrics [L, H, W, 3]
+ *   layered images (interpolated attributes, shaded colors) [L, H, W, C]
+ *   composited images [H, W, C]
+ * Batches are packed: image i's layered buffers start at element
+ * L * pixel_offset * (channels) and its composited buffer at
+ * pixel_offset * C, where pixel_offset = sum of H*W of the images before it.
+ *
+ * Reference interfaces replaced (paths inside google-research/diffren):
+ *   dr_rasterize_triangles  -> diffren::cuda::RasterizeTrianglesImpl
+ *       (diffren/common/kernels/rasterize_triangles_impl_cuda.cu.h:35-42),
+ *       reached from the XLA FFI handler rasterize_triangles
+ *       (diffren/jax/internal/kernels/rasterize_triangles_gpu.cc:44-77);
+ *       with DR_DEPTH_FLOAT it reproduces diffren::RasterizeTrianglesImpl
+ *       (rasterize_triangles_impl.h:53-58, the CPU handler of
+ *       rasterize_triangles_cpu.cc:43-79).
+ *   dr_rasterize_batch      -> jax.vmap over rasterize_triangles, which the
+ *       reference lowers to sequential per-image FFI calls
+ *       (rasterize_triangles_xla.py:68-75, vmap_method='sequential_unrolled').
+ *   dr_transform_vertices   -> transforms.transform_homogeneous
+ *       (diffren/jax/utils/transforms.py:41-79) as used by
+ *       rasterize.py:90-96 and splat.py:209-212.
+ *   dr_interpolate_fwd/bwd  -> interpolate.interpolate_vertex_attribute
+ *       (diffren/jax/internal/interpolate.py:24-63, 118-145) and its VJP.
+ *   dr_diff_barycentrics_fwd/bwd -> rasterize.differentiable_barycentrics
+ *       (diffren/jax/internal/rasterize.py:127-255) and its VJP.
+ *   dr_splat_fwd/bwd        -> splat.splat_shaded_pixels /
+ *       splat_at_pixel_centers + composite.over
+ *       (diffren/jax/internal/splat.py:26-229, diffren/jax/composite.py:20-37)
+ *       and their VJP.
+ */
+#ifndef DIFFREN_GB300_H_
+#define DIFFREN_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DR_OK 0
+#define DR_ERR_INVALID_ARGUMENT 1
+#define DR_ERR_CUDA 2
+#define DR_ERR_WORKSPACE_TOO_SMALL 3
+#define DR_ERR_MISALIGNED 4
+
+/* Values of diffren.jax.constants.FaceCullingMode (constants.py:20-24). */
+#define DR_CULL_NONE 0
+#define DR_CULL_BACK 1
+#define DR_CULL_FRONT 2
+
+/* Depth semantics of the rasterizer.
+ * DISCRETIZED: the reference CUDA rasterizer. Depth enters a packed 64-bit
+ *   key (32-bit discretized depth << 32 | triangle id); each pixel keeps the
+ *   L smallest keys. Empty layers: id 0, z 1, barycentrics 0.
+ * FLOAT: the reference CPU rasterizer. Fragments are ordered by float depth,
+ *   ties to the lower triangle id. Empty layers: id -1, z 1, barycentrics 0. */
+#define DR_DEPTH_DISCRETIZED 0
+#define DR_DEPTH_FLOAT 1
+
+/* Bits of the device error word (dr_read_error_flags). */
+#define DR_FLAG_INDEX_OUT_OF_RANGE 1u /* a triangle named a vertex >= V or < 0;
+                                         that triangle was skipped */
+
+/* One image of a batch: its mesh and its resolution. */
+typedef struct dr_image_desc {
+  int32_t width, height;
+  int32_t num_vertices, num_triangles;
+  int64_t vertex_offset;   /* first vertex of the mesh in `vertices` */
+  int64_t triangle_offset; /* first triangle of the mesh in `triangles` */
+  int64_t pixel_offset;    /* sum of width*height of the images before it */
+} dr_image_desc;
+
+typedef struct dr_raster_config {
+  int32_t num_layers;        /* L >= 1, at most DR_MAX_LAYERS */
+  int32_t face_culling_mode; /* DR_CULL_* */
+  int32_t depth_mode;        /* DR_DEPTH_* */
+  int32_t tile_width;        /* fine-raster tile, 0 = default (16) */
+  int32_t tile_height;       /* 0 = default (16); tile_width*tile_height <= 1024 */
+  int32_t large_tiles;       /* triangles spanning more tiles than this go to a
+                                per-image list every tile scans; 0 = default */
+} dr_raster_config;
+
+#define DR_MAX_LAYERS 16
+#define DR_MAX_CHANNELS 16
+#define DR_MAX_BATCH_INLINE 128 /* larger batches are split into launches */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* dr_last_error(void);
+int32_t dr_abi_version(void);
+
+/* ---------------------------------------------------------------- raster */
+
+size_t dr_rasterize_batch_workspace_bytes(const dr_image_desc* images,
+                                          int32_t num_images,
+                                          const dr_raster_config* config);
+
+/* Rasterizes every image of the batch (setup, tile binning and the
+ * shared-memory fine rasterizer run once for the whole batch). `images` is a
+ * host array. Outputs are packed [L, H_i, W_i] per image. */
+int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
+                       const dr_image_desc* images, int32_t num_images,
+                       const dr_raster_config* config, int32_t* triangle_ids,
+                       float* z_buffer, float* barycentrics, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+size_t dr_rasterize_triangles_workspace_bytes(int32_t num_triangles,
+                                              int32_t image_width,
+                                              int32_t image_height,
+                                              int32_t num_layers);
+
+/* Single image with default tiles: the drop-in for
+ * diffren::cuda::RasterizeTrianglesImpl. Unlike the reference, the
+ * barycentrics buffer is not used as scratch and indices are range-checked. */
+int dr_rasterize_triangles(const float* vertices, int32_t num_vertices,
+                           const int32_t* triangles, int32_t num_triangles,
+                           int32_t image_width, int32_t image_height,
+                           int32_t num_layers, int32_t face_culling_mode,
+                           int32_t depth_mode, int32_t* triangle_ids,
+                           float* z_buffer, float* barycentrics,
+                           void* workspace, size_t workspace_bytes,
+                           void* stream);
+
+/* Synchronizes `stream` and reads the device error word of the last raster
+ * call that used `workspace` (DR_FLAG_* bits). */
+int dr_read_error_flags(const void* workspace, uint32_t* flags, void* stream);
+
+/* ------------------------------------------------------------- transform */
+
+/* clip[v] = M_i @ (x, y, z, w or 1) for every vertex of image i, with the
+ * float32 order ((m0 x + m1 y) + m2 z) + m3 w. `matrices` is [N, 4, 4] on the
+ * device; `dim` is 3 or 4. */
+int dr_transform_vertices(const float* matrices, const float* vertices,
+                          int32_t dim, const dr_image_desc* images,
+                          int32_t num_images, float* clip_vertices,
+                          void* stream);
+
+/* VJP w.r.t. the vertices: d_vertices [V, dim] = d_clip @ M_i (written). */
+int dr_transform_vertices_bwd(const float* matrices, const float* d_clip_vertices,
+                              int32_t dim, const dr_image_desc* images,
+                              int32_t num_images, float* d_vertices, void* stream);
+
+/* --------------------------------------------------------- interpolation */
+
+/* out[l,y,x,:] = fg ? sum_i b_i * attr[tri[id][i], :] : background, where
+ * fg = (z != 1). attributes [V, K]; background [K] (nullable = zeros). */
+int dr_interpolate_fwd(const float* attributes, int32_t num_channels,
+                       const int32_t* triangles, const int32_t* triangle_ids,
+                       const float* z_buffer, const float* barycentrics,
+                       const float* background, const dr_image_desc* images,
+                       int32_t num_images, int32_t num_layers, float* out,
+                       void* stream);
+
+/* VJP. d_attributes [V, K] and d_background [K] are accumulated into (the
+ * caller zeroes them); d_barycentrics [L,H,W,3] is written when non-null. */
+int dr_interpolate_bwd(const float* d_out, const float* attributes,
+                       int32_t num_channels, const int32_t* triangles,
+                       const int32_t* triangle_ids, const float* z_buffer,
+                       const float* barycentrics, const dr_image_desc* images,
+                       int32_t num_images, int32_t num_layers,
+                       float* d_attributes, float* d_barycentrics,
+                       float* d_background, void* stream);
+
+/* ------------------------------------------- differentiable barycentrics */
+
+/* Float barycentrics from per-triangle adjugates (rasterize.py:127-255);
+ * zero where fg = 0. Output [L, H, W, 3]. */
+int dr_diff_barycentrics_fwd(const float* clip_vertices, const int32_t* triangles,
+                             const int32_t* triangle_ids, const float* z_buffer,
+                             const dr_image_desc* images, int32_t num_images,
+                             int32_t num_layers, float* barycentrics,
+                             void* stream);
+
+/* VJP: accumulates d_clip_vertices [V, 4] (caller zeroes it). */
+int dr_diff_barycentrics_bwd(const float* d_barycentrics,
+                             const float* clip_vertices, const int32_t* triangles,
+                             const int32_t* triangle_ids, const float* z_buffer,
+                             const dr_image_desc* images, int32_t num_images,
+                             int32_t num_layers, float* d_clip_vertices,
+                             void* stream);
+
+/* ----------------------------------------------------------------- splat */
+
+/* Rasterize-then-splat of shaded layers: viewport xyz from the clip-space
+ * interpolation (splat.py:207-221), 3x3 Gaussian splats with the per-tap
+ * surface test, normalization and back-to-front over compositing.
+ * colors [L,H,W,C] (C >= 1, last channel is alpha); out [H,W,C];
+ * accum and normalized [3,H,W,C] are written when non-null. */
+int dr_splat_fwd(const float* clip_vertices, const int32_t* triangles,
+                 const int32_t* triangle_ids, const float* z_buffer,
+                 const float* barycentrics, const float* colors,
+                 int32_t num_channels, const dr_image_desc* images,
+                 int32_t num_images, int32_t num_layers, float* out,
+                 float* accum, float* normalized, void* stream);
+
+/* VJP in gather form (each source splat reads the adjoints of the 9 pixels it
+ * reached; no atomics on image buffers). Writes d_colors [L,H,W,C];
+ * accumulates d_clip_vertices [V,4] (caller zeroes it); writes
+ * d_barycentrics [L,H,W,3] when non-null. */
+int dr_splat_bwd(const float* d_out, const float* clip_vertices,
+                 const int32_t* triangles, const int32_t* triangle_ids,
+                 const float* z_buffer, const float* barycentrics,
+                 const float* colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images,
+                 int32_t num_layers, float* d_colors, float* d_clip_vertices,
+                 float* d_barycentrics, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIFFREN_GB300_H_ */

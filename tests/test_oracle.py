@@ -1,0 +1,230 @@
+"""CPU tests: the oracle against the reference (compiled reference CPU
+rasterizer, committed fixtures, the reference tests' golden images and known
+answers)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import helpers
+from diffren_gb300 import workloads
+from golden import png
+from oracle import raster
+from oracle import splat as np_splat
+from oracle import torch_ref
+
+FIX = helpers.golden("raster_ref.npz")
+CASES = sorted({k.split("__")[0] for k in FIX.files})
+
+
+def _case(name):
+  g = lambda k: FIX[name + "__" + k]
+  w, h, layers, cull = (int(x) for x in g("meta"))
+  return g("vertices"), g("triangles"), w, h, layers, cull, g("ids"), g("z"), g("bary")
+
+
+def _bits(a):
+  return np.asarray(a).view(np.uint32)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_float_mode_matches_reference_fixture(name):
+  v, t, w, h, layers, cull, ids, z, bary = _case(name)
+  oi, oz, ob = raster.rasterize(v, t, w, h, layers, cull, raster.DEPTH_FLOAT)
+  np.testing.assert_array_equal(oi, ids)
+  np.testing.assert_array_equal(_bits(oz), _bits(z))
+  np.testing.assert_array_equal(_bits(ob), _bits(bary))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_discretized_mode_agrees_with_float_mode(name):
+  """Reference CUDA vs CPU semantics: same visible triangles except at
+  background (id 0 vs -1) and depth near-ties (< 2 depth quanta)."""
+  v, t, w, h, layers, cull, ids, z, bary = _case(name)
+  gi, gz, gb = raster.rasterize(v, t, w, h, layers, cull, raster.DEPTH_DISCRETIZED)
+  fg = ids >= 0
+  np.testing.assert_array_equal(gi[~fg], 0)
+  np.testing.assert_array_equal(gz[~fg], 1.0)
+  diff = fg & (gi != ids)
+  # Near ties: the float depths of the two candidates are within 2 quanta.
+  assert diff.sum() <= max(2, 0.001 * fg.sum()), diff.sum()
+  same = fg & (gi == ids)
+  np.testing.assert_allclose(gz[same], z[same], atol=2.0 / 2147483647.0 * 2, rtol=0)
+  np.testing.assert_array_equal(_bits(gb[same]), _bits(bary[same]))
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(
+    helpers.REFERENCE, "diffren/common/kernels/rasterize_triangles_impl.cc")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_matches_compiled_reference_random(seed):
+  raster.build_reference(helpers.REFERENCE)
+  rng = np.random.default_rng(100 + seed)
+  w, h = int(rng.integers(1, 90)), int(rng.integers(1, 70))
+  layers, cull = int(rng.integers(1, 6)), int(rng.integers(0, 3))
+  m = workloads.soup_workload(int(rng.integers(1, 800)), seed=seed, mu=-2.0, sigma=1.0)
+  eye = workloads.sphere_eyes(1, seed=seed, radius=float(rng.uniform(0.3, 3.0)))[0]
+  clip = raster.transform(workloads.camera_matrix(eye, w, h), m.vertices)
+  ref = raster.rasterize_reference_cpu(clip, m.triangles, w, h, layers, cull)
+  ours = raster.rasterize(clip, m.triangles, w, h, layers, cull, raster.DEPTH_FLOAT)
+  for a, b in zip(ref, ours):
+    np.testing.assert_array_equal(np.asarray(a).view(np.uint32),
+                                  np.asarray(b).view(np.uint32))
+
+
+needs_ref_data = pytest.mark.skipif(not helpers.reference_data_available(),
+                                    reason="reference test data not present")
+
+
+def _ref_png(name):
+  return png.read_png(os.path.join(helpers.REF_TEST_DATA, name))
+
+
+def _test_case(name):
+  return _case("test_" + name)[:2]
+
+
+@needs_ref_data
+@pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
+@pytest.mark.parametrize("case,golden", [
+    ("CanRasterizeTriangle", "Simple_Triangle.png"),
+    ("CanRasterizeExternalTriangle", "External_Triangle.png"),
+    ("CanRasterizeTetrahedron", "Simple_Tetrahedron.png"),
+])
+def test_oracle_golden_barycentrics(case, golden, mode):
+  """rasterize_triangles_impl_test.cc:125-168 (and the CUDA twin)."""
+  v, t = _test_case(case)
+  _, _, b = raster.rasterize(v, t, 640, 480, 1, 0, mode)
+  ok, msg = helpers.images_near_cpp(_ref_png(golden), helpers.encode_barycentrics(b))
+  assert ok, msg
+
+
+@needs_ref_data
+@pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
+def test_oracle_golden_inside_box(mode):
+  v = FIX["inside_box__vertices"]
+  t = FIX["inside_box__triangles"]
+  _, _, b = raster.rasterize(v, t, 640, 480, 1, 0, mode)
+  ok, msg = helpers.images_near_cpp(_ref_png("Inside_Box.png"),
+                                    helpers.encode_barycentrics(b))
+  assert ok, msg
+
+
+@needs_ref_data
+@pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
+def test_oracle_golden_cube_two_layers_and_culling(mode):
+  """impl_test.cc:227-294: ids and barycentrics of both layers; culling."""
+  v = FIX["cube_cull0__vertices"]
+  t = FIX["cube_cull0__triangles"]
+  # The C++ test harness zero-fills its id buffer (impl_test.cc:36-37); the
+  # -1 background of the CPU semantics comes from the XLA handler instead.
+  ids, _, b = raster.rasterize(v, t, 640, 480, 2, 0, mode)
+  ids = np.maximum(ids, 0)
+  for layer, idg, bg in ((0, "Ids_Cube.png", "Barycentrics_Cube.png"),
+                         (1, "Ids_Cube_Back.png", "Barycentrics_Cube_Back.png")):
+    ok, msg = helpers.images_near_cpp(_ref_png(idg), helpers.encode_ids(ids, layer))
+    assert ok, (idg, msg)
+    ok, msg = helpers.images_near_cpp(_ref_png(bg), helpers.encode_barycentrics(b, layer))
+    assert ok, (bg, msg)
+  empty = 0 if mode == raster.DEPTH_DISCRETIZED else -1
+  for cull, golden in ((1, "Ids_Cube_Back.png"), (2, "Ids_Cube.png")):
+    ids, _, _ = raster.rasterize(v, t, 640, 480, 2, cull, mode)
+    ok, msg = helpers.images_near_cpp(_ref_png(golden),
+                                      helpers.encode_ids(np.maximum(ids, 0), 0))
+    assert ok, (cull, msg)
+    assert (ids[1] == empty).all()
+
+
+@needs_ref_data
+def test_oracle_golden_uv_sphere_ids():
+  """rasterize_triangles_impl_cuda_test.cc:172-187 (CUDA semantics)."""
+  v, t = helpers.uv_sphere(230, 230, 0.9)
+  ids, _, _ = raster.rasterize(helpers.homogeneous(v), t, 1600, 1600, 1, 0,
+                               raster.DEPTH_DISCRETIZED)
+  ok, msg = helpers.images_near_cpp(_ref_png("UV_Sphere_Ids.png"), helpers.encode_ids(ids))
+  assert ok, msg
+
+
+@pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
+def test_oracle_edge_corner_degenerate(mode):
+  """impl_test.cc:170-225: pixel on a shared edge (both windings), image
+  corners, degenerate triangle."""
+  v = np.array([[0.0, -1.0, 0.5, 1.0], [0.0, 1.0, 0.5, 1.0], [0.5, -1.0, 0.5, 1.0]],
+               np.float32)
+  for tri in ([0, 1, 2], [2, 1, 0]):
+    _, _, b = raster.rasterize(v, np.array([tri], np.int32), 641, 480, 1, 0, mode)
+    assert abs(b[0, 5, 320].sum() - 1.0) < 1e-6
+  v = np.array([[-1, -1, 0, 1], [1, -1, 0, 1], [1, 1, 0, 1], [-1, 1, 0, 1]], np.float32)
+  _, _, b = raster.rasterize(v, np.array([[0, 1, 2], [0, 2, 3]], np.int32), 640, 480, 1,
+                             0, mode)
+  for x, y in ((0, 0), (639, 0), (639, 479), (0, 479)):
+    assert abs(b[0, y, x].sum() - 1.0) < 1e-6
+  v = np.array([[-1, -1, 0, 1], [1, 1, 0, 1], [0, 0, 0, 1]], np.float32)
+  _, _, b = raster.rasterize(v, np.array([[0, 1, 2]], np.int32), 1, 1, 1, 0, mode)
+  assert abs(b.sum()) < 1e-6
+
+
+def test_oracle_splat_two_triangles_golden():
+  """splat_test.py:47-82: composite and the 3 normalized layers."""
+  g = helpers.golden("splat_two_triangles.npz")
+  v = np.array([[-0.2, -0.2, 0, 1], [0.5, -0.2, 0, 1], [0.5, 0.5, 0, 1],
+                [0.2, -0.2, 0.5, 1], [-0.5, -0.2, 0.5, 1], [-0.5, 0.5, 0.5, 1]],
+               np.float32)
+  t = np.array([[0, 1, 2], [3, 5, 4]], np.int32)
+  colors = np.array([[0, 1, 0, 1]] * 3 + [[1, 0, 0, 1]] * 3, np.float32)
+  ids, z, b = raster.rasterize(v, t, 32, 32, 2, 1)
+  shaded = np_splat.interpolate(colors, ids, z, b, t)
+  out, _, norm = np_splat.splat_shaded_pixels(v, ids, z, b, t, shaded, 32, 32)
+  ok, msg = helpers.images_near_python(g["Composite"], helpers.pil_format(out))
+  assert ok, msg
+  for i in range(3):
+    ok, msg = helpers.images_near_python(g["Layer_%d" % i], helpers.pil_format(norm[i]))
+    assert ok, (i, msg)
+
+
+def _small_scene(seed=0, w=24, h=20, layers=3):
+  m = workloads.icosphere_workload(3, seed=seed)
+  cam = workloads.camera_matrix((0.3, 0.4, 2.4), w, h)
+  clip = raster.transform(cam, m.vertices)
+  ids, z, b = raster.rasterize(clip, m.triangles, w, h, layers, 1)
+  rng = np.random.default_rng(seed)
+  shaded = rng.uniform(0, 1, (layers, h, w, 4)).astype(np.float32)
+  return clip, m.triangles, ids, z, b, shaded, w, h
+
+
+def test_torch_oracle_matches_numpy_oracle():
+  clip, t, ids, z, b, shaded, w, h = _small_scene()
+  out, acc, norm = np_splat.splat_shaded_pixels(clip, ids, z, b, t, shaded, w, h)
+  state = torch_ref.discrete_state(clip, ids, z, b, t, w, h)
+  tout, tacc, tnorm = torch_ref.splat_shaded_pixels(
+      torch.tensor(clip), torch.tensor(ids), torch.tensor(z), torch.tensor(b),
+      torch.tensor(t), torch.tensor(shaded), w, h, state)
+  np.testing.assert_allclose(tout.numpy(), out, rtol=1e-5, atol=1e-6)
+  np.testing.assert_allclose(tacc.numpy(), acc, rtol=1e-5, atol=1e-6)
+
+
+def test_torch_oracle_gradient_matches_finite_differences():
+  """Central differences (eps 1e-3, float64) of the frozen-discrete splat."""
+  clip, t, ids, z, b, shaded, w, h = _small_scene(seed=1, w=16, h=14)
+  state = torch_ref.discrete_state(clip, ids, z, b, t, w, h)
+  ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, t))
+  target = torch.rand(h, w, 4, dtype=torch.float64, generator=torch.Generator().manual_seed(0))
+
+  def loss(c, s):
+    out = torch_ref.splat_shaded_pixels(c, ti, tz, tb.double(), tt, s, w, h, state)[0]
+    return ((out - target) ** 2).sum()
+
+  c = torch.tensor(clip, dtype=torch.float64, requires_grad=True)
+  s = torch.tensor(shaded, dtype=torch.float64, requires_grad=True)
+  gc, gs = torch.autograd.grad(loss(c, s), (c, s))
+  rng = np.random.default_rng(3)
+  used = np.unique(t[ids[z != 1.0]])
+  eps = 1e-3
+  for _ in range(16):
+    vi, k = int(rng.choice(used)), int(rng.choice([0, 1, 3]))
+    cp, cm = c.detach().clone(), c.detach().clone()
+    cp[vi, k] += eps
+    cm[vi, k] -= eps
+    fd = (loss(cp, s) - loss(cm, s)).item() / (2 * eps)
+    assert abs(fd - gc[vi, k].item()) <= 1e-4 * max(1.0, abs(fd)) + 1e-5, (vi, k, fd, gc[vi, k])

@@ -1,0 +1,217 @@
+"""GPU tests of the public API (render_triangles, rasterize_triangles with
+differentiable barycentrics), mirroring the reference's own tests:
+splat_test.py, render_test.py, interpolate_test.py, rasterize_test.py."""
+import numpy as np
+import pytest
+import torch
+
+import helpers
+from diffren_gb300 import constants, rasterize, render, workloads
+from oracle import raster
+from oracle import splat as np_splat
+
+pytestmark = pytest.mark.gpu
+
+G = helpers.golden("render_goldens.npz")
+
+
+def test_two_triangle_layers_golden(device):
+  """splat_test.py:47-82 through render_triangles."""
+  g = helpers.golden("splat_two_triangles.npz")
+  v = torch.tensor([[-0.2, -0.2, 0, 1], [0.5, -0.2, 0, 1], [0.5, 0.5, 0, 1],
+                    [0.2, -0.2, 0.5, 1], [-0.5, -0.2, 0.5, 1], [-0.5, 0.5, 0.5, 1]],
+                   device=device)
+  colors = torch.tensor([[0, 1.0, 0, 1.0]] * 3 + [[1.0, 0, 0, 1.0]] * 3, device=device)
+  out, _, norm = render.render_triangles(v, {"colors": colors}, [[0, 1, 2], [3, 5, 4]],
+                                         None, 32, 32, lambda x: x["colors"],
+                                         num_layers=2, return_accum_buffers=True)
+  ok, msg = helpers.images_near_python(g["Composite"], helpers.pil_format(out.cpu().numpy()))
+  assert ok, msg
+  for i in range(3):
+    ok, msg = helpers.images_near_python(g["Layer_%d" % i],
+                                         helpers.pil_format(norm[i].cpu().numpy()))
+    assert ok, (i, msg)
+
+
+@pytest.mark.parametrize("num_components", [4, 2])
+def test_optimize_single_triangle(num_components, device):
+  """splat_test.py:84-168: rasterize-only gradient is zero, the splat
+  gradient is not, and 15 steps halve the loss."""
+  init = torch.tensor([[[0, 0, 0, 1], [0.5, 0, 0, 1], [0.5, 0.5, 0, 1]]], device=device)
+  target_v = torch.tensor([[[-0.25, 0, 0, 1], [0.25, 0, 0, 1], [0.25, 0.5, 0, 1]]],
+                          device=device)
+  tris = torch.tensor([[0, 1, 2]], device=device)
+  colors = torch.tensor([[[0, 0.0, 0.8, 1.0], [0, 0.8, 0, 1.0], [0, 0.0, 0.8, 1.0]]],
+                        device=device)[..., -num_components:]
+
+  def render_splat(verts, do_splat):
+    return render.render_triangles(
+        verts, {"colors": colors}, tris, None, 32, 32, lambda x: x["colors"],
+        compositing_mode=(constants.CompositingMode.SPLAT_OVER if do_splat else
+                          constants.CompositingMode.OVER))
+
+  target = render_splat(target_v, False).detach()
+  var = init.clone()
+  initial = None
+  for i in range(15):
+    v = var.clone().requires_grad_(True)
+    raster_loss = ((render_splat(v, False) - target) ** 2).mean()
+    if raster_loss.requires_grad:
+      (rg,) = torch.autograd.grad(raster_loss, v, allow_unused=True)
+    else:
+      rg = None
+    splat_loss = ((render_splat(v, True) - target) ** 2).mean()
+    (sg,) = torch.autograd.grad(splat_loss, v)
+    if i == 0:
+      assert rg is None or float(rg.norm()) == pytest.approx(0.0)
+      assert float(sg.norm()) > 0.01
+      initial = float(splat_loss)
+    var = var - sg
+  final = float(((render_splat(var, True) - target) ** 2).mean())
+  assert final < 0.5 * initial, (initial, final)
+
+
+def _cube():
+  v = torch.tensor([[-1, -1, 1], [-1, -1, -1], [-1, 1, -1], [-1, 1, 1], [1, -1, 1],
+                    [1, -1, -1], [1, 1, -1], [1, 1, 1]], dtype=torch.float32)
+  t = torch.tensor([[0, 1, 2], [2, 3, 0], [3, 2, 6], [6, 7, 3], [7, 6, 5], [5, 4, 7],
+                    [4, 5, 1], [1, 0, 4], [5, 6, 2], [2, 1, 5], [7, 4, 0], [0, 3, 7]],
+                   dtype=torch.int32)
+  return v, t
+
+
+def _projections():
+  p = helpers.make_perspective_matrix()
+  return torch.tensor(np.stack([p @ helpers.make_look_at_matrix("view_1"),
+                                p @ helpers.make_look_at_matrix("view_2")]),
+                      dtype=torch.float32)
+
+
+@pytest.mark.parametrize("num_layers", [1, 2, 3])
+def test_renders_colored_cube_layers(num_layers, device):
+  """interpolate_test.py:51-75: two views (batched), NONE compositing."""
+  v, t = _cube()
+  rgba = torch.cat([v * 0.5 + 0.5, torch.ones(8, 1)], 1)
+  out = render.render_triangles(
+      v.to(device), {"rgba": rgba.to(device)}, t.to(device), _projections().to(device),
+      640, 480, lambda x: x["rgba"], num_layers=num_layers,
+      face_culling_mode=constants.FaceCullingMode.NONE,
+      compositing_mode=constants.CompositingMode.NONE)
+  for i in (0, 1):
+    for l in range(num_layers):
+      ok, msg = helpers.images_near_python(
+          G["unlit_cube_%d_%d" % (i, l)], helpers.pil_format(out[i, l].cpu().numpy()))
+      assert ok, (i, l, msg)
+
+
+@pytest.mark.parametrize("mode", ["no batching", "batched vertices", "all batched"])
+def test_renders_two_cubes_batch_modes(mode, device):
+  """render_test.py:56-98 (OVER compositing)."""
+  v, t = _cube()
+  rgba = torch.cat([v * 0.5 + 0.5, torch.ones(8, 1)], 1)
+  proj = _projections().to(device)
+  v, t, rgba = v.to(device), t.to(device), rgba.to(device)
+  if mode == "batched vertices":
+    v = v[None].expand(2, 8, 3)
+  elif mode == "all batched":
+    v, t, rgba = v[None].expand(2, 8, 3), t[None].expand(2, 12, 3), rgba[None].expand(2, 8, 4)
+  out = render.render_triangles(v, {"rgba": rgba}, t, proj, 640, 480, lambda x: x["rgba"],
+                                face_culling_mode=constants.FaceCullingMode.NONE,
+                                compositing_mode=constants.CompositingMode.OVER)
+  for i in (0, 1):
+    ok, msg = helpers.images_near_python(G["unlit_cube_%d_0" % i],
+                                         helpers.pil_format(out[i].cpu().numpy()))
+    assert ok, (i, msg)
+
+
+def test_renders_sphere_disparity(device):
+  """render_test.py:100-140: a shader that transforms world positions."""
+  v = torch.tensor(G["sphere_vertices"], device=device)
+  t = torch.tensor(G["sphere_triangles"], device=device)
+  look = torch.tensor(helpers.make_look_at_matrix("view_1"), dtype=torch.float32,
+                      device=device)
+
+  def shader(a):
+    p = a["world_position"]
+    flat = p.reshape(-1, 3)
+    cam = flat @ look[:3, :3].T + look[:3, 3]
+    disp = -1 / cam[:, 2]
+    disp = (disp - 0.12523349) / (0.16625337 - 0.12523349)
+    disp = disp.reshape(p.shape[:2])
+    return torch.stack([disp, torch.ones_like(disp)], -1)
+
+  out = render.render_triangles(v, {"world_position": v}, t, _projections()[0].to(device),
+                                640, 480, shader,
+                                compositing_mode=constants.CompositingMode.OVER)
+  ok, msg = helpers.images_near_python(helpers.to_rgba(G["sphere_disparity"])
+                                       if G["sphere_disparity"].shape[2] == 3 else
+                                       G["sphere_disparity"],
+                                       helpers.pil_format(out[..., 0:1].cpu().numpy()))
+  assert ok, msg
+
+
+def test_diff_barycentrics_known_jacobian(device):
+  """rasterize_test.py:169-227: Jacobian of the barycentrics at pixel
+  (32, 24) of a 64x48 image w.r.t. the ndc vertex coordinates."""
+  expected = helpers.golden("diff_bary_jacobian.npz")["expected"]
+  ndc = torch.tensor([[-0.5, -0.5, 0.8], [0.0, 0.5, 0.3], [0.5, -0.5, 0.3]], device=device)
+  tris = torch.tensor([[0, 1, 2]], device=device)
+  eye = torch.eye(4, device=device)
+
+  def bary(x, diff):
+    fb = rasterize.rasterize_triangles(x, tris, eye, 64, 48, compute_diff_barys=diff)
+    return fb.barycentrics[0, 24, 32, :]
+
+  jac = torch.zeros(3, 3, 3)
+  for i in range(3):
+    x = ndc.clone().requires_grad_(True)
+    (g,) = torch.autograd.grad(bary(x, True)[i], x)
+    jac[i] = g.cpu()
+  np.testing.assert_array_almost_equal(jac.numpy(), expected, decimal=6)
+  x = ndc.clone().requires_grad_(True)
+  assert not bary(x, False).requires_grad
+
+
+def test_batched_render_matches_per_image(device):
+  """A [B, ...] render equals B single renders (forward exactly, gradients
+  within tolerance)."""
+  m = workloads.icosphere_workload(6, seed=2)
+  eyes = workloads.sphere_eyes(3, seed=5)
+  cams = torch.tensor(np.stack([workloads.camera_matrix(e, 64, 48) for e in eyes]),
+                      device=device)
+  v = torch.tensor(m.vertices, device=device)
+  t = torch.tensor(m.triangles, device=device)
+  col = torch.tensor(m.colors, device=device)
+
+  def shade(a):
+    return torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1)
+
+  vb = v[None].repeat(3, 1, 1).requires_grad_(True)
+  out_b = render.render_triangles(vb, {"rgb": col}, t, cams, 64, 48, shade, num_layers=3)
+  (gb,) = torch.autograd.grad(out_b.square().sum(), vb)
+  for i in range(3):
+    vi = v.clone().requires_grad_(True)
+    out_i = render.render_triangles(vi, {"rgb": col}, t, cams[i], 64, 48, shade,
+                                    num_layers=3)
+    torch.testing.assert_close(out_b[i], out_i, rtol=0, atol=0)
+    (gi,) = torch.autograd.grad(out_i.square().sum(), vi)
+    torch.testing.assert_close(gb[i], gi, rtol=1e-4, atol=1e-5)
+
+
+def test_render_matches_oracle_pipeline(device):
+  """c1-like scene end to end: point-light-free pass-through shader,
+  forward vs the numpy oracle chain."""
+  m = workloads.icosphere_workload(16, seed=0)
+  cam = workloads.camera_matrix((0.0, 0.0, 3.0), 128, 128)
+  out = render.render_triangles(torch.tensor(m.vertices, device=device),
+                                {"rgb": torch.tensor(m.colors, device=device)},
+                                torch.tensor(m.triangles, device=device),
+                                torch.tensor(cam, device=device), 128, 128,
+                                lambda a: torch.cat([a["rgb"], torch.ones_like(
+                                    a["rgb"][..., :1])], -1), num_layers=3)
+  clip = raster.transform(cam, m.vertices)
+  ids, z, b = raster.rasterize(clip, m.triangles, 128, 128, 3, 1)
+  rgb = np_splat.interpolate(m.colors, ids, z, b, m.triangles)
+  shaded = np.concatenate([rgb, np.ones_like(rgb[..., :1])], -1)
+  ref, _, _ = np_splat.splat_shaded_pixels(clip, ids, z, b, m.triangles, shaded, 128, 128)
+  np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
