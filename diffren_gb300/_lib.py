@@ -17,6 +17,7 @@ DR_FLAG_INDEX_OUT_OF_RANGE = 1
 DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
+DR_MAX_BATCH_INLINE = 128
 
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p

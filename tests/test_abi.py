@@ -1,0 +1,118 @@
+"""CPU tests of the C ABI boundary: the library builds and loads, exports
+every symbol the header declares with the argument count the header gives,
+and rejects bad arguments without touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from diffren_gb300 import _lib, kernels
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                      "include", "diffren_gb300.h")
+
+
+def declarations():
+  src = open(HEADER).read()
+  src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+  decls = {}
+  for m in re.finditer(r"\b(dr_\w+)\s*\(([^)]*)\)\s*;", src):
+    name, params = m.groups()
+    params = params.strip()
+    n = 0 if params in ("", "void") else params.count(",") + 1
+    decls[name] = n
+  return decls
+
+
+def test_header_declares_the_boundary():
+  d = declarations()
+  for name in ("dr_rasterize_triangles", "dr_rasterize_batch", "dr_splat_fwd",
+               "dr_splat_bwd", "dr_interpolate_fwd", "dr_interpolate_bwd",
+               "dr_diff_barycentrics_fwd", "dr_diff_barycentrics_bwd",
+               "dr_transform_vertices", "dr_transform_vertices_bwd", "dr_last_error"):
+    assert name in d, name
+
+
+def test_library_exports_every_declared_symbol():
+  lib = _lib.load()
+  for name, nargs in declarations().items():
+    assert hasattr(lib, name), name
+    assert name in _lib.SIGNATURES, name
+    assert len(_lib.SIGNATURES[name][1]) == nargs, (name, nargs)
+
+
+def test_abi_version_and_error_string():
+  lib = _lib.load()
+  assert lib.dr_abi_version() == 1
+  assert isinstance(lib.dr_last_error(), bytes)
+
+
+def test_workspace_query_rejects_bad_config():
+  lib = _lib.load()
+  b = kernels.ImageBatch.single(8, 8, 3, 1)
+  for cfg in (kernels.raster_config(0, 0, 0), kernels.raster_config(17, 0, 0),
+              kernels.raster_config(1, 5, 0), kernels.raster_config(1, 0, 2),
+              kernels.raster_config(1, 0, 0, tile=(256, 8))):
+    assert lib.dr_rasterize_batch_workspace_bytes(b.ptr, 1, ctypes.byref(cfg)) == 0
+    assert lib.dr_last_error()
+  good = kernels.raster_config(3, 1, 0)
+  n = lib.dr_rasterize_batch_workspace_bytes(b.ptr, 1, ctypes.byref(good))
+  assert n > 0 and n % 256 == 0
+  assert lib.dr_rasterize_triangles_workspace_bytes(1000, 64, 64, 3) > 0
+
+
+def test_workspace_grows_with_triangles_and_tiles():
+  lib = _lib.load()
+  cfg = kernels.raster_config(3, 1, 0)
+  small = kernels.ImageBatch.single(64, 64, 3, 10)
+  big = kernels.ImageBatch.single(64, 64, 3, 10000)
+  wide = kernels.ImageBatch.single(4096, 64, 3, 10)
+  f = lambda b: lib.dr_rasterize_batch_workspace_bytes(b.ptr, 1, ctypes.byref(cfg))
+  assert f(big) > f(small) and f(wide) > f(small)
+
+
+def test_entry_points_reject_bad_arguments_without_gpu_work():
+  lib = _lib.load()
+  b = kernels.ImageBatch.single(8, 8, 3, 1)
+  cfg = kernels.raster_config(1, 0, 0)
+  # Null outputs / workspace.
+  rc = lib.dr_rasterize_batch(None, None, b.ptr, 1, ctypes.byref(cfg), None, None, None,
+                              None, 0, None)
+  assert rc == 1 and b"non-null" in lib.dr_last_error()
+  # Bad image sizes.
+  bad = kernels.ImageBatch.single(8, 8, 3, 1)
+  bad.descs[0].width = 0
+  rc = lib.dr_rasterize_batch(None, None, bad.ptr, 1, ctypes.byref(cfg), None, None,
+                              None, None, 0, None)
+  assert rc == 1
+  # Too many splat channels, bad layer counts.
+  assert lib.dr_splat_fwd(None, None, None, None, None, None, 9, b.ptr, 1, 3, None, None,
+                          None, None) == 1
+  assert lib.dr_splat_fwd(None, None, None, None, None, None, 4, b.ptr, 1, 0, None, None,
+                          None, None) == 1
+  assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
+                                None) == 1
+  assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1
+  # Misaligned clip vertices.
+  assert lib.dr_splat_fwd(ctypes.c_void_p(4), None, None, None, None, None, 4, b.ptr, 1,
+                          3, None, None, None, None) == 4
+
+
+def test_python_constants_match_header():
+  src = open(HEADER).read()
+  for name in ("DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_OK",
+               "DR_CULL_NONE", "DR_CULL_BACK", "DR_CULL_FRONT", "DR_DEPTH_DISCRETIZED",
+               "DR_DEPTH_FLOAT"):
+    m = re.search(r"#define %s (\d+)" % name, src)
+    assert m and int(m.group(1)) == getattr(_lib, name), name
+  assert kernels._groups(kernels.ImageBatch([1] * 129, [1] * 129, [0] * 129,
+                                            [0] * 129)) == 2
+
+
+def test_status_raises_with_message():
+  lib = _lib.load()
+  b = kernels.ImageBatch.single(8, 8, 3, 1)
+  lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None)
+  with pytest.raises(_lib.DiffrenError, match="dim"):
+    _lib.check(1, "dr_transform_vertices")
