@@ -18,6 +18,7 @@ DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
 DR_MAX_BATCH_INLINE = 128
+DR_STATIC_SCRATCH_BYTES = 64 << 20
 
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p
@@ -48,6 +49,8 @@ SIGNATURES = {
     "dr_rasterize_triangles_workspace_bytes": (_S, [_I, _I, _I, _I]),
     "dr_rasterize_triangles": (_I, [_P, _I, _P, _I, _I, _I, _I, _I, _I, _P, _P,
                                     _P, _P, _S, _P]),
+    "dr_rasterize_triangles_static_scratch": (_I, [_P, _I, _P, _I, _I, _I, _I, _I,
+                                                   _I, _P, _P, _P, _P]),
     "dr_read_error_flags": (_I, [_P, _P, _P]),
     "dr_transform_vertices": (_I, [_P, _P, _I, _P, _I, _P, _P]),
     "dr_transform_vertices_bwd": (_I, [_P, _P, _I, _P, _I, _P, _P]),

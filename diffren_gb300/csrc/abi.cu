@@ -43,6 +43,10 @@ dr_raster_config default_config(int32_t L, int32_t cull, int32_t depth_mode) {
 
 }  // namespace
 
+namespace dr {
+void set_last_error(const std::string& msg) { g_error = msg; }
+}  // namespace dr
+
 extern "C" {
 
 const char* dr_last_error(void) { return g_error.c_str(); }

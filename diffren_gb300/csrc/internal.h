@@ -60,6 +60,9 @@ inline int launch_status(const char* what, std::string& err) {
   return DR_ERR_CUDA;
 }
 
+// abi.cu: message returned by dr_last_error() on this thread.
+void set_last_error(const std::string& msg);
+
 // raster.cu
 size_t raster_workspace_bytes(const dr_image_desc* images, int n,
                               const dr_raster_config* cfg, std::string& err);

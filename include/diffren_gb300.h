@@ -134,6 +134,24 @@ int dr_rasterize_triangles(const float* vertices, int32_t num_vertices,
                            void* workspace, size_t workspace_bytes,
                            void* stream);
 
+/* Allocation-free variant of dr_rasterize_triangles (no counterpart in the
+ * reference). It is for callers that cannot allocate device memory for
+ * scratch space, such as an XLA custom-call handler, which gets only its
+ * input and result buffers from XLA. The scratch lives in a static device
+ * array of DR_STATIC_SCRATCH_BYTES inside this library, which every GPU that
+ * loads the library holds until exit; requests that need more return
+ * DR_ERR_WORKSPACE_TOO_SMALL without running anything. The first call on a
+ * device looks up the array's device address (once per device, with that
+ * device current); make that first call before any stream capture. All
+ * calls share the array, so calls that overlap on the GPU race: order them
+ * (e.g. one stream). The call itself allocates nothing. */
+#define DR_STATIC_SCRATCH_BYTES (64u << 20)
+int dr_rasterize_triangles_static_scratch(
+    const float* vertices, int32_t num_vertices, const int32_t* triangles,
+    int32_t num_triangles, int32_t image_width, int32_t image_height,
+    int32_t num_layers, int32_t face_culling_mode, int32_t depth_mode,
+    int32_t* triangle_ids, float* z_buffer, float* barycentrics, void* stream);
+
 /* Synchronizes `stream` and reads the device error word of the last raster
  * call that used `workspace` (DR_FLAG_* bits). */
 int dr_read_error_flags(const void* workspace, uint32_t* flags, void* stream);
