@@ -4,7 +4,8 @@ Workload (default `c5`): a ragged batch of 64 seeded meshes (noisy
 icospheres or triangle soups, 50/50), triangle counts lognormal (median 20k,
 sigma 1.2) clipped to [500, 500k], one camera per mesh on a sphere of radius
 3, square resolutions drawn from {256, 512, 1024}, 3 depth layers, back-face
-culling, RGB vertex colors shaded to RGBA (alpha 1). One step = forward
+culling, RGB vertex colors with alpha 1 interpolated as an RGBA attribute and
+passed through by the deferred shader. One step = forward
 render of every image + L2 loss against fixed target images + backward to
 vertex positions and vertex colors.
 
@@ -45,7 +46,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
   ap = argparse.ArgumentParser()
   ap.add_argument("--gpus", type=int, default=1)
-  ap.add_argument("--steps", type=int, default=10)
+  ap.add_argument("--steps", type=int, default=100)
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
   ap.add_argument("--workload", default="c5", choices=["c5", "c2", "c3", "c1"])
@@ -98,9 +99,20 @@ class Workload:
 
 
 def shader(a):
+  """Pass-through of the interpolated RGBA vertex colors (the reference's
+  render tests shade with `lambda x: x['rgba']` the same way)."""
+  return a["rgba"]
+
+
+def rgba(colors):
+  """Per-vertex RGBA from RGB with alpha 1 (differentiable w.r.t. RGB)."""
   import torch
-  rgb = a["rgb"]
-  return torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+  return torch.cat([colors, torch.ones_like(colors[:, :1])], 1)
+
+
+def l2_loss(out, target):
+  import torch.nn.functional as F
+  return F.mse_loss(out, target, reduction="sum")
 
 
 # ----------------------------------------------------------------- clocks
@@ -131,6 +143,16 @@ class ClockSampler:
     for line in self.proc.stdout:
       self.lines.append(line.strip())
 
+  def wait_for_samples(self, n=2, timeout=5.0):
+    """Blocks until the sampler has produced n lines (or timeout)."""
+    t0 = time.time()
+    while self.proc is not None and len(self.lines) < n and time.time() - t0 < timeout:
+      time.sleep(0.05)
+
+  def mark(self):
+    """Index of the next sample; samples from here on are in the region."""
+    return len(self.lines)
+
   def __exit__(self, *a):
     if self.proc is not None:
       self.proc.terminate()
@@ -139,10 +161,11 @@ class ClockSampler:
       except subprocess.TimeoutExpired:
         self.proc.kill()
 
-  def summary(self):
+  def summary(self, start=0):
     sm, mx, reasons = [], [], set()
     names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-    for ln in self.lines:
+    lines = self.lines[start:] or self.lines[-1:]
+    for ln in lines:
       p = [x.strip() for x in ln.split(",")]
       if len(p) < 9:
         continue
@@ -161,23 +184,27 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- our arm
-def kernel_bytes(wl, batch, ids_z, C=4, K=3):
+def kernel_bytes(wl, C=4, K=4):
   """Algorithmic (compulsory) HBM bytes per launch of each kernel."""
   L, P = wl.num_layers, wl.pixels
   T = wl.triangles
-  fg = int(ids_z)  # foreground layer-pixels of the step
   return {
       # indices + 3 gathered clip vertices per triangle, ids + z + bary out
       "raster": T * (12 + 48) + 20 * L * P,
-      # per layer-pixel: ids, z, bary in (20 B) + K floats out
+      # per layer sample: ids, z, bary in (20 B) + K floats out
       "interp_fwd": L * P * (20 + 4 * K),
-      # per layer-pixel: ids, z, bary, color (20 + 4C) in; composited C out
-      "splat_fwd": L * P * (20 + 4 * C) + 4 * C * P,
-      # d_out in; ids, z, bary, color in; d_color out
-      "splat_bwd": 4 * C * P + L * P * (20 + 4 * C) + L * P * 4 * C,
-      # per layer-pixel: ids, z, bary, d_attr in (fg only gather-scatter)
+      # per layer sample: ids, z, bary in; viewport xyz + fg out (16 B)
+      "splat_positions": L * P * (20 + 16),
+      # per layer sample: position (16 B) + color in; per pixel: composited
+      # color and the saved accumulators (3 (C + 1) floats) out
+      "splat_fwd": L * P * (16 + 4 * C) + P * (4 * C + 12 * (C + 1)),
+      # per pixel: saved accumulators + d_out in; per layer sample: position
+      # and color in, d color and d position out
+      "splat_bwd": P * (12 * (C + 1) + 4 * C) + L * P * (16 + 4 * C + 4 * C + 16),
+      # per layer sample: d position, ids, z, bary in (vertex scatter to L2)
+      "splat_positions_bwd": L * P * (16 + 20),
+      # per layer sample: ids, z, bary, d attribute in
       "interp_bwd": L * P * (20 + 4 * K),
-      "fg_layer_pixels": fg,
   }
 
 
@@ -205,8 +232,8 @@ def run_ours(args, rank, world, device):
   def step():
     v = verts.detach().requires_grad_(True)
     c = cols.detach().requires_grad_(True)
-    out = r.render(v, {"rgb": c}, cams, shader)
-    loss = (out - target).square().sum()
+    out = r.render(v, {"rgba": rgba(c)}, cams, shader)
+    loss = l2_loss(out, target)
     gv, gc = torch.autograd.grad(loss, (v, c))
     g_v.copy_(gv)
     g_c.copy_(gc)
@@ -250,8 +277,11 @@ def run_ours(args, rank, world, device):
     return ms
 
   with ClockSampler(device.index) as clocks:
+    clocks.wait_for_samples()
+    start = clocks.mark()
     ms = timed(graph.replay, args.steps)
-  clock = clocks.summary()
+    time.sleep(0.25)  # let the sample that covers the region's end arrive
+  clock = clocks.summary(start)
   loss_val = float(loss_out)
 
   # e2e: public API with host buffers; H2D inputs and D2H loss + grads.
@@ -300,9 +330,9 @@ def run_plain(wl, device, args):
     for v0, c0, tri, cam, w, h, tgt in data:
       v = v0.detach().requires_grad_(True)
       c = c0.detach().requires_grad_(True)
-      out = render.render_triangles(v, {"rgb": c}, tri, cam, w, h, shader,
+      out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
                                     num_layers=wl.num_layers)
-      loss = (out - tgt).square().sum()
+      loss = l2_loss(out, tgt)
       torch.autograd.grad(loss, (v, c))
 
   for _ in range(2):
@@ -347,10 +377,9 @@ def cpu_port_sample(wl, budget_s, threads):
     tc = torch.tensor(clip, requires_grad=True)
     tcol = torch.tensor(m.colors, requires_grad=True)
     ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
-    rgb = torch_ref.interpolate(tcol, ti, tz, tb, tt)
-    shaded = torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+    shaded = torch_ref.interpolate(rgba(tcol), ti, tz, tb, tt)
     out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
-    loss = (out - torch.tensor(tgt)).square().sum()
+    loss = l2_loss(out, torch.tensor(tgt))
     torch.autograd.grad(loss, (tc, tcol))
     t_total += time.perf_counter() - t0
     px += w * h
@@ -429,9 +458,8 @@ def main():
     return
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
-  dom = max((k for k in pk if k in ("raster", "interp_fwd", "splat_fwd", "splat_bwd",
-                                    "interp_bwd")), key=lambda k: pk[k])
-  nbytes = kernel_bytes(wl, res["renderer"].batch, 0)
+  nbytes = kernel_bytes(wl)
+  dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
   value = world * wl.pixels / res["ms"] / 1e3
   line = {

@@ -52,6 +52,7 @@ SIGNATURES = {
     "dr_rasterize_triangles_static_scratch": (_I, [_P, _I, _P, _I, _I, _I, _I, _I,
                                                    _I, _P, _P, _P, _P]),
     "dr_read_error_flags": (_I, [_P, _P, _P]),
+    "dr_selftest_depth_codec": (_I, [_P, _P]),
     "dr_transform_vertices": (_I, [_P, _P, _I, _P, _I, _P, _P]),
     "dr_transform_vertices_bwd": (_I, [_P, _P, _I, _P, _I, _P, _P]),
     "dr_interpolate_fwd": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
@@ -59,10 +60,10 @@ SIGNATURES = {
                                 _P, _P]),
     "dr_diff_barycentrics_fwd": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_diff_barycentrics_bwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
-    "dr_splat_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P,
-                          _P]),
-    "dr_splat_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P,
-                          _P, _P]),
+    "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
+    "dr_splat_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
+    "dr_splat_bwd": (_I, [_P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),
 }
 
 _lib = None

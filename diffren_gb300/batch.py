@@ -94,8 +94,8 @@ class BatchRenderer:
     shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
     shaded = shaded.reshape(-1, shaded.shape[-1])
     if compositing_mode == constants.CompositingMode.SPLAT_OVER:
-      return kernels.splat_packed(clip, shaded, bary, self.triangles, ids, z, b, L,
-                                  return_accum_buffers)
+      vp = kernels.splat_positions_packed(clip, bary, self.triangles, ids, z, b, L)
+      return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers)
     fg = (z != 1.0).float()[:, None]
     shaded = shaded * fg
     if compositing_mode == constants.CompositingMode.NONE:

@@ -113,6 +113,11 @@ int dr_read_error_flags(const void* workspace, uint32_t* flags, void* stream) {
   return DR_OK;
 }
 
+int dr_selftest_depth_codec(unsigned long long* results, void* stream) {
+  std::string err;
+  return finish(dr::depth_codec_selftest(results, as_stream(stream), err), err);
+}
+
 int dr_transform_vertices(const float* matrices, const float* vertices, int32_t dim,
                           const dr_image_desc* images, int32_t num_images,
                           float* clip_vertices, void* stream) {
@@ -183,30 +188,50 @@ int dr_diff_barycentrics_bwd(const float* d_barycentrics, const float* clip_vert
                 err);
 }
 
-int dr_splat_fwd(const float* clip_vertices, const int32_t* triangles,
-                 const int32_t* triangle_ids, const float* z_buffer,
-                 const float* barycentrics, const float* colors, int32_t num_channels,
-                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
-                 float* out, float* accum, float* normalized, void* stream) {
+int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
+                           const int32_t* triangle_ids, const float* z_buffer,
+                           const float* barycentrics, const dr_image_desc* images,
+                           int32_t num_images, int32_t num_layers, float* positions,
+                           void* stream) {
   std::string err;
-  return finish(dr::splat_fwd_launch(clip_vertices, triangles, triangle_ids, z_buffer,
-                                     barycentrics, colors, num_channels, images,
-                                     num_images, num_layers, out, accum, normalized,
+  return finish(dr::positions_fwd_launch(clip_vertices, triangles, triangle_ids, z_buffer,
+                                         barycentrics, images, num_images, num_layers,
+                                         positions, as_stream(stream), err),
+                err);
+}
+
+int dr_splat_positions_bwd(const float* d_positions, const float* clip_vertices,
+                           const int32_t* triangles, const int32_t* triangle_ids,
+                           const float* z_buffer, const float* barycentrics,
+                           const dr_image_desc* images, int32_t num_images,
+                           int32_t num_layers, float* d_clip_vertices,
+                           float* d_barycentrics, void* stream) {
+  std::string err;
+  return finish(dr::positions_bwd_launch(d_positions, clip_vertices, triangles,
+                                         triangle_ids, z_buffer, barycentrics, images,
+                                         num_images, num_layers, d_clip_vertices,
+                                         d_barycentrics, as_stream(stream), err),
+                err);
+}
+
+int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* out, float* saved, float* accum, float* normalized, void* stream) {
+  std::string err;
+  return finish(dr::splat_fwd_launch(positions, colors, num_channels, images, num_images,
+                                     num_layers, out, saved, accum, normalized,
                                      as_stream(stream), err),
                 err);
 }
 
-int dr_splat_bwd(const float* d_out, const float* clip_vertices,
-                 const int32_t* triangles, const int32_t* triangle_ids,
-                 const float* z_buffer, const float* barycentrics, const float* colors,
-                 int32_t num_channels, const dr_image_desc* images, int32_t num_images,
-                 int32_t num_layers, float* d_colors, float* d_clip_vertices,
-                 float* d_barycentrics, void* stream) {
+int dr_splat_bwd(const float* d_out, const float* positions, const float* colors,
+                 const float* saved, int32_t num_channels, const dr_image_desc* images,
+                 int32_t num_images, int32_t num_layers, float* d_colors,
+                 float* d_positions, void* stream) {
   std::string err;
-  return finish(dr::splat_bwd_launch(d_out, clip_vertices, triangles, triangle_ids,
-                                     z_buffer, barycentrics, colors, num_channels, images,
-                                     num_images, num_layers, d_colors, d_clip_vertices,
-                                     d_barycentrics, as_stream(stream), err),
+  return finish(dr::splat_bwd_launch(d_out, positions, colors, saved, num_channels, images,
+                                     num_images, num_layers, d_colors, d_positions,
+                                     as_stream(stream), err),
                 err);
 }
 

@@ -39,6 +39,27 @@ __device__ __forceinline__ int find_segment(const T* start, int n, T key) {
   return lo;
 }
 
+// One (layer, pixel) element of a packed layered batch buffer: flat index q
+// runs over every image's L x H x W elements in image order.
+struct PixelRef {
+  int img;
+  int64_t e;    // element index in the packed layered buffers
+  int64_t pix;  // pixel index inside its image (y * W + x)
+  int x, y;
+};
+
+__device__ __forceinline__ PixelRef decode(const Batch& B, int L, int64_t q) {
+  PixelRef r;
+  r.img = find_segment(B.pix_prefix, B.n, q / L);
+  const int64_t hw = int64_t(B.width[r.img]) * B.height[r.img];
+  const int64_t local = q - int64_t(L) * B.pix_prefix[r.img];
+  r.e = int64_t(L) * B.pix_off[r.img] + local;
+  r.pix = local % hw;
+  r.y = int(r.pix / B.width[r.img]);
+  r.x = int(r.pix - int64_t(r.y) * B.width[r.img]);
+  return r;
+}
+
 // ------------------------------------------------------------ exact math
 // Float-to-integer conversions round toward zero, saturate and map NaN to 0
 // (cvt.rzi); int64-to-float rounds to nearest. The CPU checker implements
@@ -185,12 +206,119 @@ __device__ __forceinline__ float fragment_z(const float b[3], float3 vz, float3 
 }
 
 // DiscretizeZ / UndiscretizeZ (rasterize_triangles_impl_cuda.cu.cc:143-159):
-// scale = uint32 max / 2 as an integer, arithmetic in double.
-__device__ __forceinline__ uint32_t discretize_z(float z) {
+// scale S = uint32 max / 2 as an integer (2^31 - 1), arithmetic in double.
+// These are the reference formulas; the rasterizer uses the integer
+// emulations below (GB300's FP64 rate made them its bottleneck), and
+// dr_selftest_depth_codec checks the two against each other on every input.
+__device__ __forceinline__ uint32_t discretize_z_fp64(float z) {
   return __double2uint_rz(__dmul_rn(__dadd_rn((double)z, 1.0), 2147483647.0));
 }
-__device__ __forceinline__ float undiscretize_z(uint32_t d) {
+__device__ __forceinline__ float undiscretize_z_fp64(uint32_t d) {
   return __double2float_rn(__dsub_rn(__ddiv_rn((double)d, 2147483647.0), 1.0));
+}
+
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ int bitlen128(u128 x) {
+  const uint64_t hi = uint64_t(x >> 64), lo = uint64_t(x);
+  return hi ? 128 - __clzll(hi) : (lo ? 64 - __clzll(lo) : 0);
+}
+
+// Rounds x to a multiple of 2^g, ties to even (g >= 1).
+__device__ __forceinline__ u128 round_bits_even(u128 x, int g) {
+  const u128 one = 1;
+  const u128 rem = x & ((one << g) - 1), half = one << (g - 1);
+  u128 q = x >> g;
+  if (rem > half || (rem == half && (q & 1))) q += 1;
+  return q << g;
+}
+
+// x / 2^s rounded to nearest, ties to even (s >= 0), for x < 2^24.
+__device__ __forceinline__ uint64_t shift_round_even(uint64_t x, int s) {
+  if (s == 0) return x;
+  if (s >= 64) return 0;  // x < 2^24 < half
+  const uint64_t q = x >> s, rem = x & ((1ull << s) - 1), half = 1ull << (s - 1);
+  return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
+// Exact integer form of discretize_z_fp64 for z in [-1, 1] or NaN:
+// a = RN_double(z + 1) as N * 2^-sh, then floor(RN_double(a * S)).
+__device__ __forceinline__ uint32_t discretize_z(float z) {
+  const uint32_t bits = __float_as_uint(z);
+  const uint32_t mag = bits & 0x7fffffffu;
+  if (mag > 0x7f800000u) return discretize_z_fp64(z);  // NaN: the hardware's conversion
+  if (mag == 0) return 2147483647u;  // (0 + 1) * S
+  const bool neg = bits >> 31;
+  const int bexp = int(mag >> 23);
+  const uint64_t M = bexp ? ((mag & 0x7fffffu) | 0x800000u) : (mag & 0x7fffffu);
+  const int E = bexp ? bexp - 150 : -149;  // |z| = M * 2^E
+  uint64_t N;
+  int sh;
+  if (E >= -52) {  // 1 + z has at most 53 significant bits: exact
+    sh = -E;
+    N = neg ? (1ull << sh) - M : (1ull << sh) + M;
+  } else if (!neg) {  // 1 + z in (1, 1 + 2^-29): ulp 2^-52
+    sh = 52;
+    N = (1ull << 52) + shift_round_even(M, -52 - E);
+  } else {  // 1 + z in (1 - 2^-29, 1): ulp 2^-53
+    sh = 53;
+    N = (1ull << 53) - shift_round_even(M, -53 - E);
+  }
+  u128 Q = u128(N) * 2147483647u;  // a * S = Q * 2^-sh exactly
+  const int bl = bitlen128(Q);
+  if (bl > 53) Q = round_bits_even(Q, bl - 53);
+  return uint32_t(Q >> sh);
+}
+
+// Exact integer form of undiscretize_z_fp64: q = RN_double(d / S) from the
+// repeating base-2^31 expansion of d / S, r = RN_double(q - 1), then
+// RN_float(r). Fixed point in units of 2^-83 (q >= 1/S has ulp >= 2^-83).
+__device__ __forceinline__ float undiscretize_z(uint32_t d) {
+  const uint32_t S = 2147483647u;
+  const u128 one = 1;
+  const uint32_t I = (d >= S) + (d >= 2 * S);
+  const uint64_t e = d - uint64_t(I) * S;  // d / S = I + e / S, e < S
+  u128 Qf;  // q in units of 2^-83
+  if (e == 0) {
+    Qf = u128(I) << 83;
+  } else {
+    // floor(e / S * 2^93) = e * (2^62 + 2^31 + 1); the remainder is nonzero,
+    // so rounding never ties.
+    const u128 F = (u128(e) << 62) | (u128(e) << 31) | u128(e);
+    if (I == 0) {
+      const int n = 64 - __clzll(e);
+      const int g = n + 9;  // keep 53 bits below F's leading bit n + 61
+      const u128 q = (F >> g) + ((F >> (g - 1)) & 1);
+      Qf = q << (n - 1);  // q * 2^(g - 93) in 2^-83 units
+    } else if (I == 1) {
+      const u128 q = (((one << 93) + F) >> 41) + ((F >> 40) & 1);
+      Qf = q << 31;  // q * 2^-52
+    } else {  // d = 2S + 1 only: q in (2, 3), ulp 2^-51
+      const u128 q = (((one << 94) + F) >> 42) + ((F >> 41) & 1);
+      Qf = q << 32;
+    }
+  }
+  // r = q - 1: exact for q >= 1/2; otherwise |r| in (1/2, 1] rounds to a
+  // multiple of 2^-53 (2^30 units).
+  const u128 one83 = one << 83;
+  bool rneg;
+  u128 R;
+  if (Qf >= one83) {
+    rneg = false;
+    R = Qf - one83;
+  } else {
+    rneg = true;
+    R = one83 - Qf;
+    if (Qf < (one << 82)) R = round_bits_even(R, 30);
+  }
+  if (R == 0) return 0.0f;
+  const int bl = bitlen128(R);
+  if (bl > 24) R = round_bits_even(R, bl - 24);
+  const int bl2 = bitlen128(R);
+  const int g = bl2 > 24 ? bl2 - 24 : 0;
+  const float mant = float(uint32_t(R >> g));  // exact (< 2^24)
+  const float v = ldexpf(mant, g - 83);
+  return rneg ? -v : v;
 }
 
 // Order-preserving float -> uint32 map with -0 == +0 (float depth keys).

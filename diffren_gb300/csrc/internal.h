@@ -70,6 +70,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
                   const dr_image_desc* images, int n, const dr_raster_config* cfg,
                   int32_t* ids, float* z, float* bary, void* workspace,
                   size_t ws_bytes, cudaStream_t stream, std::string& err);
+int depth_codec_selftest(unsigned long long* out, cudaStream_t stream, std::string& err);
 // Byte offset of the device error word inside a raster workspace.
 constexpr size_t kErrorFlagsOffset = 4;
 
@@ -98,15 +99,21 @@ int diffbary_bwd_launch(const float* d_bary, const float* clip, const int32_t* t
                         cudaStream_t stream, std::string& err);
 
 // splat.cu
-int splat_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
-                     const float* z, const float* bary, const float* colors, int C,
-                     const dr_image_desc* images, int n, int L, float* out,
+int positions_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
+                         const float* z, const float* bary, const dr_image_desc* images,
+                         int n, int L, float* positions, cudaStream_t stream,
+                         std::string& err);
+int positions_bwd_launch(const float* d_positions, const float* clip, const int32_t* tris,
+                         const int32_t* ids, const float* z, const float* bary,
+                         const dr_image_desc* images, int n, int L, float* d_clip,
+                         float* d_bary, cudaStream_t stream, std::string& err);
+int splat_fwd_launch(const float* positions, const float* colors, int C,
+                     const dr_image_desc* images, int n, int L, float* out, float* saved,
                      float* accum, float* normalized, cudaStream_t stream,
                      std::string& err);
-int splat_bwd_launch(const float* d_out, const float* clip, const int32_t* tris,
-                     const int32_t* ids, const float* z, const float* bary,
-                     const float* colors, int C, const dr_image_desc* images, int n,
-                     int L, float* d_colors, float* d_clip, float* d_bary,
-                     cudaStream_t stream, std::string& err);
+int splat_bwd_launch(const float* d_out, const float* positions, const float* colors,
+                     const float* saved, int C, const dr_image_desc* images, int n, int L,
+                     float* d_colors, float* d_positions, cudaStream_t stream,
+                     std::string& err);
 
 }  // namespace dr

@@ -13,26 +13,6 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Decodes flat index q over all images' [L, H, W] elements.
-struct PixelRef {
-  int img;
-  int64_t e;    // element index in the packed layered buffers
-  int64_t pix;  // pixel index inside its image (y * W + x)
-  int x, y;
-};
-
-__device__ __forceinline__ PixelRef decode(const Batch& B, int L, int64_t q) {
-  PixelRef r;
-  r.img = find_segment(B.pix_prefix, B.n, q / L);
-  const int64_t hw = int64_t(B.width[r.img]) * B.height[r.img];
-  const int64_t local = q - int64_t(L) * B.pix_prefix[r.img];
-  r.e = int64_t(L) * B.pix_off[r.img] + local;
-  r.pix = local % hw;
-  r.y = int(r.pix / B.width[r.img]);
-  r.x = int(r.pix - int64_t(r.y) * B.width[r.img]);
-  return r;
-}
-
 __device__ __forceinline__ int3 load_tri(const int32_t* tris, const Batch& B, int img,
                                          int id) {
   const int32_t* t = tris + 3 * (B.triangle_offset[img] + id);

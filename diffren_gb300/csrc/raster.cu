@@ -395,6 +395,36 @@ __global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Bat
   }
 }
 
+// Compares the integer depth codec with the reference's double formulas on
+// every input: all 2^32 discretized values, and every float in [-1, 1]
+// plus NaNs. out: [0] discretize mismatches, [1] first bad float bits,
+// [2] undiscretize mismatches, [3] first bad discretized value, [4] the
+// discretized value of a NaN depth, [5] / [6] the int32 / int64 conversion
+// of a NaN float (toward zero).
+__global__ void depth_codec_selftest_kernel(unsigned long long* out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const float nan = __uint_as_float(0x7fc00000u);
+    out[4] = discretize_z_fp64(nan);
+    out[5] = (unsigned long long)(unsigned)__float2int_rz(nan);
+    out[6] = (unsigned long long)__float2ll_rz(nan);
+  }
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (1ull << 32);
+       i += stride) {
+    const uint32_t u = uint32_t(i);
+    if (__float_as_uint(undiscretize_z(u)) != __float_as_uint(undiscretize_z_fp64(u))) {
+      atomicAdd(&out[2], 1ull);
+      atomicMin(&out[3], (unsigned long long)u);
+    }
+    const float z = __uint_as_float(u);
+    const bool in_domain = (z != z) || (z >= -1.0f && z <= 1.0f);
+    if (in_domain && discretize_z(z) != discretize_z_fp64(z)) {
+      atomicAdd(&out[0], 1ull);
+      atomicMin(&out[1], (unsigned long long)u);
+    }
+  }
+}
+
 int resolve_tile(int v) { return v > 0 ? v : kDefaultTile; }
 
 bool check_config(const dr_raster_config* cfg, int& L, int& TW, int& TH, int& large,
@@ -421,6 +451,15 @@ bool check_config(const dr_raster_config* cfg, int& L, int& TW, int& TH, int& la
 }
 
 }  // namespace
+
+int depth_codec_selftest(unsigned long long* out, cudaStream_t stream, std::string& err) {
+  if (!out) { err = "results buffer is null"; return DR_ERR_INVALID_ARGUMENT; }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  depth_codec_selftest_kernel<<<sms * 8, 256, 0, stream>>>(out);
+  return launch_status("depth codec self-test", err);
+}
 
 size_t raster_workspace_bytes(const dr_image_desc* images, int n,
                               const dr_raster_config* cfg, std::string& err) {

@@ -386,24 +386,67 @@ def diff_barycentrics_packed(clip, triangles, ids, z, batch, num_layers):
 
 
 # ------------------------------------------------------------------ splat
+class _Positions(torch.autograd.Function):
+  """Viewport xyz + foreground flag of every layer sample (splat.py:207-221)."""
+
+  @staticmethod
+  def forward(ctx, clip, bary, triangles, ids, z, batch, L):
+    lib = _lib.load()
+    vp = torch.empty(ids.shape[0], 4, dtype=torch.float32, device=ids.device)
+    with _op("splat_positions", _groups(batch)):
+      rc = lib.dr_splat_positions_fwd(_p(clip), _p(triangles), _p(ids), _p(z), _p(bary),
+                                      batch.ptr, batch.n, L, _p(vp), _stream(ids.device))
+    _lib.check(rc, "dr_splat_positions_fwd")
+    ctx.save_for_backward(clip, bary, triangles, ids, z)
+    ctx.batch, ctx.L = batch, L
+    return vp
+
+  @staticmethod
+  def backward(ctx, d_vp):
+    clip, bary, triangles, ids, z = ctx.saved_tensors
+    lib = _lib.load()
+    d_vp = d_vp.contiguous()
+    if d_vp.data_ptr() % 16:
+      d_vp = d_vp.clone()
+    d_clip = torch.zeros_like(clip) if ctx.needs_input_grad[0] else None
+    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[1] else None
+    if d_clip is None and d_bary is None:
+      return None, None, None, None, None, None, None
+    scratch = d_clip if d_clip is not None else torch.zeros_like(clip)
+    with _op("splat_positions_bwd", _groups(ctx.batch)):
+      rc = lib.dr_splat_positions_bwd(_p(d_vp), _p(clip), _p(triangles), _p(ids), _p(z),
+                                      _p(bary), ctx.batch.ptr, ctx.batch.n, ctx.L,
+                                      _p(scratch), _p(d_bary), _stream(d_vp.device))
+    _lib.check(rc, "dr_splat_positions_bwd")
+    return d_clip, d_bary, None, None, None, None, None
+
+
+def splat_positions_packed(clip, bary, triangles, ids, z, batch, num_layers):
+  """[L*P, 4] viewport positions (x, y, z, fg) of a packed batch."""
+  return _Positions.apply(clip, bary, triangles, ids, z, batch, num_layers)
+
+
 class _Splat(torch.autograd.Function):
 
   @staticmethod
-  def forward(ctx, clip, colors, bary, triangles, ids, z, batch, L, want_accum):
+  def forward(ctx, positions, colors, batch, L, want_accum):
     lib = _lib.load()
     C = colors.shape[1]
     dev = colors.device
-    out = torch.empty(batch.total_pixels, C, dtype=torch.float32, device=dev)
+    P = batch.total_pixels
+    out = torch.empty(P, C, dtype=torch.float32, device=dev)
+    needs_grad = positions.requires_grad or colors.requires_grad
+    saved = (torch.empty(P, 3 * (C + 1), dtype=torch.float32, device=dev)
+             if needs_grad else None)
     accum = norm = None
     if want_accum:
-      accum = torch.empty(3 * batch.total_pixels, C, dtype=torch.float32, device=dev)
+      accum = torch.empty(3 * P, C, dtype=torch.float32, device=dev)
       norm = torch.empty_like(accum)
     with _op("splat_fwd", _groups(batch)):
-      rc = lib.dr_splat_fwd(_p(clip), _p(triangles), _p(ids), _p(z), _p(bary),
-                          _p(colors), C, batch.ptr, batch.n, L, _p(out), _p(accum),
-                          _p(norm), _stream(dev))
+      rc = lib.dr_splat_fwd(_p(positions), _p(colors), C, batch.ptr, batch.n, L, _p(out),
+                            _p(saved), _p(accum), _p(norm), _stream(dev))
     _lib.check(rc, "dr_splat_fwd")
-    ctx.save_for_backward(clip, colors, bary, triangles, ids, z)
+    ctx.save_for_backward(positions, colors, saved)
     ctx.batch, ctx.L = batch, L
     if want_accum:
       ctx.mark_non_differentiable(accum, norm)
@@ -412,35 +455,37 @@ class _Splat(torch.autograd.Function):
 
   @staticmethod
   def backward(ctx, d_out, *unused):
-    clip, colors, bary, triangles, ids, z = ctx.saved_tensors
+    positions, colors, saved = ctx.saved_tensors
     lib = _lib.load()
     d_out = d_out.contiguous()
+    if d_out.data_ptr() % 16:
+      d_out = d_out.clone()
     d_colors = torch.empty_like(colors)
-    d_clip = torch.zeros_like(clip)
-    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[2] else None
+    d_pos = torch.empty_like(positions)
     with _op("splat_bwd", _groups(ctx.batch)):
-      rc = lib.dr_splat_bwd(_p(d_out), _p(clip), _p(triangles), _p(ids), _p(z),
-                          _p(bary), _p(colors), colors.shape[1], ctx.batch.ptr,
-                          ctx.batch.n, ctx.L, _p(d_colors), _p(d_clip), _p(d_bary),
-                          _stream(d_out.device))
+      rc = lib.dr_splat_bwd(_p(d_out), _p(positions), _p(colors), _p(saved),
+                            colors.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L,
+                            _p(d_colors), _p(d_pos), _stream(d_out.device))
     _lib.check(rc, "dr_splat_bwd")
-    return (d_clip if ctx.needs_input_grad[0] else None, d_colors, d_bary, None,
-            None, None, None, None, None)
+    return (d_pos if ctx.needs_input_grad[0] else None,
+            d_colors if ctx.needs_input_grad[1] else None, None, None, None)
 
 
-def splat_packed(clip, colors, bary, triangles, ids, z, batch, num_layers,
-                 return_accum_buffers=False):
+def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False):
   """Splatted, normalized, composited images [P, C] of a packed batch.
 
-  With ``return_accum_buffers`` also returns the accumulated and normalized
+  positions [L*P, 4] (viewport xyz, fg) and colors [L*P, C]. With
+  ``return_accum_buffers`` also returns the accumulated and normalized
   fg/surface/bg layers, packed [3, H_i, W_i, C] per image (not
   differentiable).
   """
   colors = colors.contiguous()
   if colors.dtype != torch.float32:
     colors = colors.float()
+  if colors.data_ptr() % 16:
+    colors = colors.clone()
   if colors.shape[1] > _lib.DR_MAX_SPLAT_CHANNELS:
     raise ValueError("splatting supports at most %d channels" %
                      _lib.DR_MAX_SPLAT_CHANNELS)
-  return _Splat.apply(clip, colors, bary, triangles, ids, z, batch, num_layers,
-                      bool(return_accum_buffers))
+  positions = positions.contiguous()
+  return _Splat.apply(positions, colors, batch, num_layers, bool(return_accum_buffers))

@@ -1,10 +1,12 @@
-"""Rasterize-then-splat (diffren/jax/internal/splat.py:178-229).
+"""Rasterize-then-splat (diffren/jax/internal/splat.py).
 
 ``splat_shaded_pixels`` re-derives the splat positions from the vertices by
 interpolating clip coordinates with the rasterized barycentrics (so the
-gradient reaches the vertices), splats every shaded layer sample to its 3x3
-neighbourhood with the per-tap surface test, normalizes and composites, all
-in one CUDA kernel; the VJP is the gather-form kernel (see csrc/splat.cu).
+gradient reaches the vertices, splat.py:207-221), then
+``splat_at_pixel_centers`` splats every shaded layer sample to its 3x3
+neighbourhood with the per-tap surface test, normalizes and composites
+(splat.py:26-175). Each step is a CUDA kernel with a hand-written VJP (see
+csrc/splat.cu).
 """
 import torch
 
@@ -13,7 +15,7 @@ from . import kernels
 from . import rasterize as rasterize_lib
 
 
-def _shaded_flat(shaded, frame):
+def _shaded_flat(shaded):
   C = shaded.shape[-1]
   s = shaded.reshape(-1, C)
   if s.dtype != torch.float32:
@@ -21,20 +23,42 @@ def _shaded_flat(shaded, frame):
   return s.contiguous()
 
 
-def splat_clip(clip, frame: fb.Framebuffer, shaded_pixels, return_accum_buffers=False):
-  """Splat with precomputed clip-space vertices (packed like the framebuffer)."""
-  batch, tris, ids, z, bary = frame.kernel_inputs()
-  colors = _shaded_flat(shaded_pixels, frame)
-  res = kernels.splat_packed(clip, colors, bary, tris, ids, z, batch, frame.num_layers,
-                             return_accum_buffers)
-  H, W = frame.height, frame.width
-  C = colors.shape[1]
-  lead = (frame.batch_size,) if frame.is_batched else ()
+def _shape_outputs(res, lead, H, W, C, return_accum_buffers):
   if return_accum_buffers:
     out, accum, norm = res
     return (out.view(*lead, H, W, C), accum.view(*lead, 3, H, W, C),
             norm.view(*lead, 3, H, W, C))
   return res.view(*lead, H, W, C)
+
+
+def splat_at_pixel_centers(xyz_layers, color_layers, foreground_mask):
+  """Splats layered samples onto the pixel grid (splat.py:26-175).
+
+  xyz_layers [L, H, W, 3] viewport positions, color_layers [L, H, W, C]
+  (last channel alpha), foreground_mask [L, H, W, 1]. Returns the
+  composited [H, W, C] image and the accumulated and normalized
+  [3, H, W, C] fg/surface/bg buffers, like the reference. Differentiable
+  w.r.t. the xy positions and the colors (the mask and the z used by the
+  surface test carry no gradient, as in the reference).
+  """
+  L, H, W, C = color_layers.shape
+  fg = torch.as_tensor(foreground_mask, device=color_layers.device).float()
+  vp = torch.cat([xyz_layers.float(), fg.reshape(L, H, W, 1).detach()], -1)
+  batch = kernels.ImageBatch.single(W, H, 0, 0)
+  res = kernels.splat_packed(vp.reshape(-1, 4), _shaded_flat(color_layers), batch, L,
+                             return_accum_buffers=True)
+  return _shape_outputs(res, (), H, W, C, True)
+
+
+def splat_clip(clip, frame: fb.Framebuffer, shaded_pixels, return_accum_buffers=False):
+  """Splat with precomputed clip-space vertices (packed like the framebuffer)."""
+  batch, tris, ids, z, bary = frame.kernel_inputs()
+  colors = _shaded_flat(shaded_pixels)
+  vp = kernels.splat_positions_packed(clip, bary, tris, ids, z, batch, frame.num_layers)
+  res = kernels.splat_packed(vp, colors, batch, frame.num_layers, return_accum_buffers)
+  lead = (frame.batch_size,) if frame.is_batched else ()
+  return _shape_outputs(res, lead, frame.height, frame.width, colors.shape[1],
+                        return_accum_buffers)
 
 
 def splat_shaded_pixels(vertices, camera_matrices, rasterized_fb: fb.Framebuffer,

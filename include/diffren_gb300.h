@@ -36,9 +36,10 @@
  *       (diffren/jax/internal/interpolate.py:24-63, 118-145) and its VJP.
  *   dr_diff_barycentrics_fwd/bwd -> rasterize.differentiable_barycentrics
  *       (diffren/jax/internal/rasterize.py:127-255) and its VJP.
- *   dr_splat_fwd/bwd        -> splat.splat_shaded_pixels /
- *       splat_at_pixel_centers + composite.over
- *       (diffren/jax/internal/splat.py:26-229, diffren/jax/composite.py:20-37)
+ *   dr_splat_positions_fwd/bwd -> the clip-space interpolation and viewport
+ *       transform of splat.splat_shaded_pixels (splat.py:207-221) and its VJP.
+ *   dr_splat_fwd/bwd        -> splat.splat_at_pixel_centers + composite.over
+ *       (diffren/jax/internal/splat.py:26-175, diffren/jax/composite.py:20-37)
  *       and their VJP.
  */
 #ifndef DIFFREN_GB300_H_
@@ -156,6 +157,17 @@ int dr_rasterize_triangles_static_scratch(
  * call that used `workspace` (DR_FLAG_* bits). */
 int dr_read_error_flags(const void* workspace, uint32_t* flags, void* stream);
 
+/* Self-test of the rasterizer's depth codec: the integer emulation of the
+ * reference's double-precision DiscretizeZ / UndiscretizeZ
+ * (rasterize_triangles_impl_cuda.cu.cc:143-159) against those formulas on
+ * every input. `results` is 7 device uint64s the caller initializes to
+ * {0, UINT64_MAX, 0, UINT64_MAX, 0, 0, 0}; on completion they hold the
+ * discretize mismatch count, the first bad float bit pattern, the
+ * undiscretize mismatch count, the first bad discretized value, the
+ * discretized value of a NaN depth, and the float-to-int32 and
+ * float-to-int64 conversions of NaN on this GPU. */
+int dr_selftest_depth_codec(unsigned long long* results, void* stream);
+
 /* ------------------------------------------------------------- transform */
 
 /* clip[v] = M_i @ (x, y, z, w or 1) for every vertex of image i, with the
@@ -212,29 +224,48 @@ int dr_diff_barycentrics_bwd(const float* d_barycentrics,
 
 /* ----------------------------------------------------------------- splat */
 
-/* Rasterize-then-splat of shaded layers: viewport xyz from the clip-space
- * interpolation (splat.py:207-221), 3x3 Gaussian splats with the per-tap
- * surface test, normalization and back-to-front over compositing.
- * colors [L,H,W,C] (C >= 1, last channel is alpha); out [H,W,C];
- * accum and normalized [3,H,W,C] are written when non-null. */
-int dr_splat_fwd(const float* clip_vertices, const int32_t* triangles,
-                 const int32_t* triangle_ids, const float* z_buffer,
-                 const float* barycentrics, const float* colors,
-                 int32_t num_channels, const dr_image_desc* images,
-                 int32_t num_images, int32_t num_layers, float* out,
-                 float* accum, float* normalized, void* stream);
+#define DR_MAX_SPLAT_CHANNELS 8
 
-/* VJP in gather form (each source splat reads the adjoints of the 9 pixels it
- * reached; no atomics on image buffers). Writes d_colors [L,H,W,C];
- * accumulates d_clip_vertices [V,4] (caller zeroes it); writes
- * d_barycentrics [L,H,W,3] when non-null. */
-int dr_splat_bwd(const float* d_out, const float* clip_vertices,
-                 const int32_t* triangles, const int32_t* triangle_ids,
-                 const float* z_buffer, const float* barycentrics,
-                 const float* colors, int32_t num_channels,
-                 const dr_image_desc* images, int32_t num_images,
-                 int32_t num_layers, float* d_colors, float* d_clip_vertices,
-                 float* d_barycentrics, void* stream);
+/* Viewport positions of every layer sample for splatting (splat.py:207-221):
+ * clip xyzw interpolated with the barycentrics (background (0, 0, 1, 1)),
+ * viewport = ((xyz / w + 1) * (W, H, 1)) * 0.5, with fg = (z != 1) in the
+ * fourth component. positions [L, H, W, 4], 16-byte aligned. */
+int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
+                           const int32_t* triangle_ids, const float* z_buffer,
+                           const float* barycentrics, const dr_image_desc* images,
+                           int32_t num_images, int32_t num_layers, float* positions,
+                           void* stream);
+
+/* VJP of dr_splat_positions_fwd w.r.t. the viewport x, y (viewport z only
+ * enters comparisons): accumulates d_clip_vertices [V, 4] (caller zeroes
+ * it) and writes d_barycentrics [L, H, W, 3] when non-null. */
+int dr_splat_positions_bwd(const float* d_positions, const float* clip_vertices,
+                           const int32_t* triangles, const int32_t* triangle_ids,
+                           const float* z_buffer, const float* barycentrics,
+                           const dr_image_desc* images, int32_t num_images,
+                           int32_t num_layers, float* d_clip_vertices,
+                           float* d_barycentrics, void* stream);
+
+/* splat_at_pixel_centers + composite.over (splat.py:26-175,
+ * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the
+ * per-tap surface test, normalization and back-to-front over compositing.
+ * positions [L, H, W, 4] (viewport xyz, fg); colors [L, H, W, C]
+ * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
+ * saved [H, W, 3, C + 1] receives the fg/surface/bg accumulators and
+ * weights the VJP needs (nullable); accum and normalized [3, H, W, C] are
+ * the reference's debugging buffers (nullable). With C % 4 == 0 the color
+ * and output buffers must be 16-byte aligned. */
+int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* out, float* saved, float* accum, float* normalized, void* stream);
+
+/* VJP in gather form: each sample reads the adjoints of the 9 pixels it
+ * reached (no atomics). Writes d_colors [L, H, W, C] and d_positions
+ * [L, H, W, 4] as (d x, d y, 0, 0). `saved` is the forward's. */
+int dr_splat_bwd(const float* d_out, const float* positions, const float* colors,
+                 const float* saved, int32_t num_channels, const dr_image_desc* images,
+                 int32_t num_images, int32_t num_layers, float* d_colors,
+                 float* d_positions, void* stream);
 
 #ifdef __cplusplus
 }

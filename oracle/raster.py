@@ -17,6 +17,11 @@ _REF_SO = os.path.join(_HERE, "_ref", "libref_raster.so")
 
 DEPTH_DISCRETIZED = 0  # reference CUDA rasterizer semantics
 DEPTH_FLOAT = 1  # reference CPU rasterizer semantics
+# What the GPU's toward-zero conversions give a NaN input (the rules
+# raster_oracle.c implements; checked by the GPU depth-codec self-test).
+NAN_TO_U32_FROM_DOUBLE = 0x80000000
+NAN_TO_I32 = 0
+NAN_TO_I64 = -0x8000000000000000
 
 _lib = None
 _ref = None

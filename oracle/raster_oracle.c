@@ -22,8 +22,11 @@
  *     in id order and inserts on strict '<'). Empty layers: id -1, z 1,
  *     barycentrics 0.
  *
- * Float-to-integer conversions saturate and map NaN to 0 (the CUDA cvt.rzi
- * rule), so that this file gives the same bits on x86-64 and aarch64.
+ * Float-to-integer conversions saturate out-of-range values and map NaN as
+ * the GPU's cvt.rzi does (float to int32: 0; float to int64: INT64_MIN;
+ * double to uint32, the depth conversion: 0x80000000), so that this file
+ * gives the same bits on
+ * x86-64 and aarch64 and matches the CUDA rasterizer.
  */
 #include <math.h>
 #include <stdint.h>
@@ -44,14 +47,14 @@ static int f2i_sat(float f) {
 }
 
 static fx_t f2l_sat(float f) {
-  if (f != f) return 0;
+  if (f != f) return INT64_MIN;
   if (f >= 9223372036854775808.0f) return INT64_MAX;
   if (f < -9223372036854775808.0f) return INT64_MIN;
   return (fx_t)f;
 }
 
 static uint32_t d2u_sat(double d) {
-  if (d != d) return 0;
+  if (d != d) return 0x80000000u;
   if (d >= 4294967296.0) return UINT32_MAX;
   if (d <= 0.0) return 0;
   return (uint32_t)d;

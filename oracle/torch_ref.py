@@ -37,10 +37,17 @@ def viewport_xyz(clip, ids, z, bary, triangles, width, height):
 
 
 def discrete_state(clip32, ids, z, bary32, triangles, width, height):
-  """float32 floor(xy) [L,H,W,2] and surface masks [L, 9, 3, H, W] (numpy)."""
+  """float32 floor(xy) [L,H,W,2] and surface masks [L, 9, 3, H+2, W+2]."""
   xyz = np_splat.viewport_xyz(clip32, ids, z, bary32, triangles, width, height)
-  L, H, W, _ = xyz.shape
-  floors = np.floor(xyz[..., :2])
+  return np.floor(xyz[..., :2]), discrete_state_xyz(xyz, None)
+
+
+def discrete_state_xyz(xyz, fg):
+  """Surface masks [L, 9, 3, H+2, W+2] of float32 viewport positions: for
+  each layer and tap (u, v), one-hot over (in front, at, behind) the
+  surface (splat.py:124-154)."""
+  xyz = np.asarray(xyz, np.float32)
+  L, H, W = xyz.shape[:3]
   zpad = np.pad(xyz[..., 2:3], ((0, 0), (1, 1), (1, 1), (0, 0)), constant_values=1.0)
   masks = np.zeros((L, 9, 3, H + 2, W + 2), np.float32)
   for l in range(L):
@@ -52,7 +59,7 @@ def discrete_state(clip32, ids, z, bary32, triangles, width, height):
       dt = np.abs(zpad - tapz[0])
       surf = np.where(np.min(dt, 0) < np.min(dc, 0), -np.argmin(dt, 0), np.argmin(dc, 0))
       masks[l, j] = np.stack([(surf > l), (surf == l), (surf < l)])[..., 0]
-  return floors, masks
+  return masks
 
 
 def _max0(x):

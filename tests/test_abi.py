@@ -87,16 +87,18 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
                               None, None, 0, None)
   assert rc == 1
   # Too many splat channels, bad layer counts.
-  assert lib.dr_splat_fwd(None, None, None, None, None, None, 9, b.ptr, 1, 3, None, None,
-                          None, None) == 1
-  assert lib.dr_splat_fwd(None, None, None, None, None, None, 4, b.ptr, 1, 0, None, None,
-                          None, None) == 1
+  assert lib.dr_splat_fwd(None, None, 9, b.ptr, 1, 3, None, None, None, None, None) == 1
+  assert lib.dr_splat_fwd(None, None, 4, b.ptr, 1, 0, None, None, None, None, None) == 1
+  # The backward needs the forward's saved accumulators.
+  assert lib.dr_splat_bwd(None, None, None, None, 4, b.ptr, 1, 3, None, None, None) == 1
   assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
                                 None) == 1
   assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1
-  # Misaligned clip vertices.
-  assert lib.dr_splat_fwd(ctypes.c_void_p(4), None, None, None, None, None, 4, b.ptr, 1,
-                          3, None, None, None, None) == 4
+  # Misaligned positions / clip vertices.
+  assert lib.dr_splat_fwd(ctypes.c_void_p(4), None, 4, b.ptr, 1, 3, None, None, None,
+                          None, None) == 4
+  assert lib.dr_splat_positions_fwd(ctypes.c_void_p(4), None, None, None, None, b.ptr, 1,
+                                    3, None, None) == 4
 
 
 def test_python_constants_match_header():

@@ -117,6 +117,24 @@ def test_c2_full_size_matches_oracle(device):
   assert_same(ours, ref)
 
 
+def test_depth_codec_matches_double_formulas_exhaustively(device):
+  """The integer depth codec equals the reference's double-precision
+  DiscretizeZ / UndiscretizeZ on all 2^32 inputs (every float in [-1, 1]
+  and NaN for the first)."""
+  res = torch.tensor([0, -1, 0, -1, 0, 0, 0], dtype=torch.int64, device=device)
+  rc = _lib.load().dr_selftest_depth_codec(ctypes.c_void_p(res.data_ptr()),
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+  assert rc == 0
+  r = res.cpu().numpy().view(np.uint64)
+  assert r[0] == 0, "discretize mismatches: %d, first input bits %#x" % (r[0], r[1])
+  assert r[2] == 0, "undiscretize mismatches: %d, first input %d" % (r[2], r[3])
+  # NaN conversions are what the CPU checker assumes.
+  got = (int(r[4]), int(r[5]) & 0xffffffff, int(r[6]))
+  want = (raster.NAN_TO_U32_FROM_DOUBLE, raster.NAN_TO_I32 & 0xffffffff,
+          raster.NAN_TO_I64 & 0xffffffffffffffff)
+  assert got == want, [hex(x) for x in got]
+
+
 def test_empty_and_degenerate_inputs(device):
   # No triangles: every layer is background.
   ids, z, b = run_abi(np.zeros((3, 4), np.float32), np.zeros((0, 3), np.int32), 9, 7, 2,

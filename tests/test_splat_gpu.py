@@ -100,13 +100,15 @@ def test_interpolate_backward_matches_autograd(case, device):
 
 def run_splat(device, clip, tris, ids, z, b, shaded, w, h, layers, accum=False,
               requires_grad=False):
+  """Positions + splat through the C ABI; returns (clip, colors, result)."""
   c, t, i, zz, bb, s = to_dev(device, clip, tris, ids.reshape(-1), z.reshape(-1),
                               b.reshape(-1, 3), shaded.reshape(-1, shaded.shape[-1]))
   if requires_grad:
     c.requires_grad_(True)
     s.requires_grad_(True)
   batch = kernels.ImageBatch.single(w, h, len(clip), len(tris))
-  res = kernels.splat_packed(c, s, bb, t, i, zz, batch, layers, accum)
+  vp = kernels.splat_positions_packed(c, bb, t, i, zz, batch, layers)
+  res = kernels.splat_packed(vp, s, batch, layers, accum)
   return c, s, res
 
 
@@ -142,6 +144,52 @@ def test_splat_backward_matches_autograd(case, device):
   dc, ds = torch.autograd.grad(o, (c, s), torch.as_tensor(g, device=device).view(o.shape))
   assert_grad_close(ds.view(layers, h, w, C).cpu().numpy(), gs.numpy())
   assert_grad_close(dc.cpu().numpy(), gc.numpy())
+
+
+def test_splat_positions_match_oracle(device):
+  clip, tris, ids, z, b, shaded, _ = scene("shells", 40, 36, 3, 4, 3)
+  ref = np_splat.viewport_xyz(clip, ids, z, b, tris, 40, 36)
+  c, t, i, zz, bb = to_dev(device, clip, tris, ids.reshape(-1), z.reshape(-1),
+                           b.reshape(-1, 3))
+  batch = kernels.ImageBatch.single(40, 36, len(clip), len(tris))
+  vp = kernels.splat_positions_packed(c, bb, t, i, zz, batch, 3).view(3, 36, 40, 4)
+  np.testing.assert_array_equal(vp[..., :3].cpu().numpy(), ref)
+  np.testing.assert_array_equal(vp[..., 3].cpu().numpy(), (z != 1).astype(np.float32))
+
+
+@pytest.mark.parametrize("C", [4, 3])
+def test_splat_at_pixel_centers_off_center_positions(C, device):
+  """The public splat_at_pixel_centers on samples that sit off the pixel
+  centres (so every tap weight differs), forward and VJP w.r.t. xy."""
+  from diffren_gb300 import splat as splat_lib
+  rng = np.random.default_rng(7)
+  L, H, W = 3, 19, 23
+  ys, xs = np.meshgrid(np.arange(H) + 0.5, np.arange(W) + 0.5, indexing="ij")
+  xyz = np.stack([np.broadcast_to(xs, (L, H, W)), np.broadcast_to(ys, (L, H, W)),
+                  np.sort(rng.uniform(0, 1, (L, H, W)), axis=0)], -1).astype(np.float32)
+  xyz[..., :2] += rng.uniform(-0.3, 0.3, (L, H, W, 2)).astype(np.float32)
+  fg = (rng.uniform(0, 1, (L, H, W, 1)) < 0.8).astype(np.float32)
+  col = rng.uniform(0, 1, (L, H, W, C)).astype(np.float32)
+  out, acc, norm = np_splat.splat_at_pixel_centers(xyz, col, fg)
+  tx = torch.tensor(xyz, device=device, requires_grad=True)
+  tc = torch.tensor(col, device=device, requires_grad=True)
+  o, a, n = splat_lib.splat_at_pixel_centers(tx, tc, torch.tensor(fg, device=device))
+  np.testing.assert_allclose(o.detach().cpu().numpy(), out, rtol=FWD_RTOL, atol=FWD_ATOL)
+  np.testing.assert_allclose(a.cpu().numpy(), acc, rtol=FWD_RTOL, atol=FWD_ATOL)
+  np.testing.assert_allclose(n.cpu().numpy(), norm, rtol=FWD_RTOL, atol=FWD_ATOL)
+  g = rng.standard_normal((H, W, C)).astype(np.float32)
+  dx, dc = torch.autograd.grad(o, (tx, tc), torch.tensor(g, device=device))
+  # float64 autograd with the float32 discrete decisions held fixed.
+  floors = np.floor(xyz[..., :2])
+  state = torch_ref.discrete_state_xyz(xyz, fg)
+  rx = torch.tensor(xyz, dtype=torch.float64, requires_grad=True)
+  rc = torch.tensor(col, dtype=torch.float64, requires_grad=True)
+  ro = torch_ref.splat_at_pixel_centers(rx, rc, torch.tensor(fg, dtype=torch.float64),
+                                        floors, state)[0]
+  gx, gc = torch.autograd.grad(ro, (rx, rc), torch.tensor(g, dtype=torch.float64))
+  assert_grad_close(dc.cpu().numpy(), gc.numpy())
+  assert_grad_close(dx[..., :2].cpu().numpy(), gx[..., :2].numpy())
+  assert float(dx[..., 2].abs().max()) == 0.0
 
 
 def test_splat_two_triangles_golden(device):
