@@ -203,6 +203,11 @@ def kernel_bytes(wl, C=4, K=4):
       "splat_bwd": P * (12 * (C + 1) + 4 * C) + L * P * (16 + 4 * C + 4 * C + 16),
       # per layer sample: d position, ids, z, bary in (vertex scatter to L2)
       "splat_positions_bwd": L * P * (16 + 20),
+      # fused interpolation + positions: ids, z, bary in; K floats and the
+      # position out
+      "samples_fwd": L * P * (20 + 4 * K + 16),
+      # its VJP: ids, z, bary, d attribute and d position in
+      "samples_bwd": L * P * (20 + 4 * K + 16),
       # per layer sample: ids, z, bary, d attribute in
       "interp_bwd": L * P * (20 + 4 * K),
   }

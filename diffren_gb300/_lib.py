@@ -60,6 +60,10 @@ SIGNATURES = {
                                 _P, _P]),
     "dr_diff_barycentrics_fwd": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_diff_barycentrics_bwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "dr_interpolate_with_positions_fwd": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I, _I,
+                                              _P, _P, _P]),
+    "dr_interpolate_with_positions_bwd": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P,
+                                              _I, _I, _P, _P, _P, _P]),
     "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),

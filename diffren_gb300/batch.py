@@ -7,8 +7,9 @@ needs equal shapes. ``BatchRenderer`` instead packs a fixed ragged batch
 (per-mesh triangle lists and per-image resolutions) once, keeps its own
 rasterizer workspace, and renders all images with one launch sequence:
 transform, setup + tile binning + the persistent fine rasterizer over the
-batch's (image, tile) queue, interpolation, the user's shader on the packed
-buffers, splat/normalize/composite, and the VJP kernels. Because no call
+batch's (image, tile) queue, interpolation fused with the splat positions,
+the user's shader on the packed buffers, splat/normalize/composite, and the
+VJP kernels. Because no call
 allocates outside torch's allocator or synchronizes, a whole forward+backward
 step can be captured in a CUDA graph (``torch.cuda.graph``) and replayed.
 
@@ -89,12 +90,16 @@ class BatchRenderer:
     parts = [kernels._f32(attributes[k], self.device) for k in keys]
     widths = [p.shape[1] for p in parts]
     cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0]
-    interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
+    splatting = compositing_mode == constants.CompositingMode.SPLAT_OVER
+    if splatting:
+      interp, vp = kernels.interpolate_with_positions_packed(cat, clip, bary,
+                                                             self.triangles, ids, z, b, L)
+    else:
+      interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
     split = torch.split(interp, widths, dim=1)
     shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
     shaded = shaded.reshape(-1, shaded.shape[-1])
-    if compositing_mode == constants.CompositingMode.SPLAT_OVER:
-      vp = kernels.splat_positions_packed(clip, bary, self.triangles, ids, z, b, L)
+    if splatting:
       return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers)
     fg = (z != 1.0).float()[:, None]
     shaded = shaded * fg

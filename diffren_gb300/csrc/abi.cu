@@ -188,6 +188,39 @@ int dr_diff_barycentrics_bwd(const float* d_barycentrics, const float* clip_vert
                 err);
 }
 
+int dr_interpolate_with_positions_fwd(const float* attributes, int32_t num_channels,
+                                      const float* clip_vertices, const int32_t* triangles,
+                                      const int32_t* triangle_ids, const float* z_buffer,
+                                      const float* barycentrics, const dr_image_desc* images,
+                                      int32_t num_images, int32_t num_layers,
+                                      float* attributes_out, float* positions, void* stream) {
+  std::string err;
+  return finish(dr::samples_fwd_launch(attributes, num_channels, clip_vertices, triangles,
+                                       triangle_ids, z_buffer, barycentrics, images,
+                                       num_images, num_layers, attributes_out, positions,
+                                       as_stream(stream), err),
+                err);
+}
+
+int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
+                                      const float* d_positions, const float* attributes,
+                                      int32_t num_channels, const float* clip_vertices,
+                                      const int32_t* triangles, const int32_t* triangle_ids,
+                                      const float* z_buffer, const float* barycentrics,
+                                      const dr_image_desc* images, int32_t num_images,
+                                      int32_t num_layers, float* d_attributes,
+                                      float* d_clip_vertices, float* d_barycentrics,
+                                      void* stream) {
+  std::string err;
+  return finish(dr::samples_bwd_launch(d_attributes_out, d_positions, attributes,
+                                       num_channels, clip_vertices, triangles,
+                                       triangle_ids, z_buffer, barycentrics, images,
+                                       num_images, num_layers, d_attributes,
+                                       d_clip_vertices, d_barycentrics, as_stream(stream),
+                                       err),
+                err);
+}
+
 int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
                            const int32_t* triangle_ids, const float* z_buffer,
                            const float* barycentrics, const dr_image_desc* images,

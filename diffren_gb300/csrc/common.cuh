@@ -246,7 +246,10 @@ __device__ __forceinline__ uint64_t shift_round_even(uint64_t x, int s) {
 __device__ __forceinline__ uint32_t discretize_z(float z) {
   const uint32_t bits = __float_as_uint(z);
   const uint32_t mag = bits & 0x7fffffffu;
-  if (mag > 0x7f800000u) return discretize_z_fp64(z);  // NaN: the hardware's conversion
+  // NaN: (NaN + 1) * S converts to 0x80000000 on the GPU (checked against
+  // discretize_z_fp64 by dr_selftest_depth_codec). A constant keeps the
+  // double-precision path out of the rasterizer entirely.
+  if (mag > 0x7f800000u) return 0x80000000u;
   if (mag == 0) return 2147483647u;  // (0 + 1) * S
   const bool neg = bits >> 31;
   const int bexp = int(mag >> 23);

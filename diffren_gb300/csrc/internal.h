@@ -99,6 +99,17 @@ int diffbary_bwd_launch(const float* d_bary, const float* clip, const int32_t* t
                         cudaStream_t stream, std::string& err);
 
 // splat.cu
+int samples_fwd_launch(const float* attributes, int K, const float* clip,
+                       const int32_t* tris, const int32_t* ids, const float* z,
+                       const float* bary, const dr_image_desc* images, int n, int L,
+                       float* attr_out, float* positions, cudaStream_t stream,
+                       std::string& err);
+int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
+                       const float* attributes, int K, const float* clip,
+                       const int32_t* tris, const int32_t* ids, const float* z,
+                       const float* bary, const dr_image_desc* images, int n, int L,
+                       float* d_attributes, float* d_clip, float* d_bary,
+                       cudaStream_t stream, std::string& err);
 int positions_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
                          const float* z, const float* bary, const dr_image_desc* images,
                          int n, int L, float* positions, cudaStream_t stream,

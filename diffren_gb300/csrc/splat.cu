@@ -1,10 +1,13 @@
 // Rasterize-then-splat for GB300 (diffren/jax/internal/splat.py:26-229,
-// diffren/jax/composite.py:20-37) and its VJP, as four kernels:
+// diffren/jax/composite.py:20-37) and its VJP:
 //
 //   positions_fwd  per layer sample: clip xyzw interpolated with the
 //                  rasterized barycentrics (background (0, 0, 1, 1)),
 //                  projected to viewport xyz, plus the foreground flag
 //                  (splat.py:207-221) -> float4 per sample.
+//   samples_fwd    the same pass fused with the interpolation of the vertex
+//                  attributes (interpolate.py:24-63): one triangle lookup and
+//                  one set of vertex gathers feed both outputs.
 //   splat_fwd      screen tiles with a 1-pixel halo of samples in shared
 //                  memory; each output pixel gathers the splats of its 3x3
 //                  neighbours and every layer with the per-tap surface test,
@@ -16,6 +19,7 @@
 //                  pixels it reached -> d colors and d viewport xy. No atomics.
 //   positions_bwd  d viewport -> d clip vertices (float atomics over the
 //                  triangle's three vertices) and d barycentrics.
+//   samples_bwd    positions_bwd fused with the attribute VJP.
 //
 // With positions computed once, neither splat kernel gathers triangle data,
 // and the backward never recomputes the forward accumulation.
@@ -126,14 +130,166 @@ __global__ void __launch_bounds__(256) positions_bwd_kernel(PosArgs a, Batch B) 
   }
 }
 
+// ------------------------------------------- fused attributes + positions
+// One pass per layer sample that both interpolates vertex attributes
+// (interpolate.py:24-63, background 0) and computes the splat position: the
+// triangle lookup, barycentrics and vertex gathers are shared. The render
+// paths use it; results equal interp_fwd_kernel and positions_fwd_kernel.
+struct SampleArgs {
+  PosArgs pos;
+  const float* attr;  // [V, K]
+  int K;
+  float* attr_out;         // [L*P, K]
+  const float* d_attr_out;  // backward input (nullable)
+  float* d_attr;            // [V, K] accumulated
+};
+
+// Channels k0 .. k0 + n - 1 (n <= 4) of a row; `vec` when the row is
+// 16-byte aligned and holds 4 channels from k0.
+__device__ __forceinline__ float4 load_chunk(const float* p, int n, bool vec) {
+  if (vec) return __ldg(reinterpret_cast<const float4*>(p));
+  float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  v.x = __ldg(p);
+  if (n > 1) v.y = __ldg(p + 1);
+  if (n > 2) v.z = __ldg(p + 2);
+  if (n > 3) v.w = __ldg(p + 3);
+  return v;
+}
+
+__device__ __forceinline__ void store_chunk(float* p, float4 v, int n, bool vec) {
+  if (vec) {
+    *reinterpret_cast<float4*>(p) = v;
+    return;
+  }
+  p[0] = v.x;
+  if (n > 1) p[1] = v.y;
+  if (n > 2) p[2] = v.z;
+  if (n > 3) p[3] = v.w;
+}
+
+__device__ __forceinline__ void add_chunk(float* p, float4 v, int n, bool vec) {
+  if (vec) {
+    atomicAdd(reinterpret_cast<float4*>(p), v);
+    return;
+  }
+  atomicAdd(p, v.x);
+  if (n > 1) atomicAdd(p + 1, v.y);
+  if (n > 2) atomicAdd(p + 2, v.z);
+  if (n > 3) atomicAdd(p + 3, v.w);
+}
+
+// (a0 b0 + a1 b1) + a2 b2 per channel (interpolate.py:24-63).
+__device__ __forceinline__ float lerp3(float a0, float a1, float a2, const float b[3]) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b[0]), __fmul_rn(a1, b[1])), __fmul_rn(a2, b[2]));
+}
+
+__global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B) {
+  const PosArgs& p = a.pos;
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= int64_t(p.L) * B.pix_prefix[B.n]) return;
+  const PixelRef r = decode(B, p.L, q);
+  const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
+  const int K = a.K;
+  const bool vec_rows = (K & 3) == 0;
+  float4 c = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
+  float fg = 0.0f;
+  float* o = a.attr_out + r.e * K;
+  if (__ldg(p.z + r.e) != 1.0f) {
+    fg = 1.0f;
+    const Interp it = interpolate_clip(p, B, r.img, r.e);
+    c = it.c;
+    const float* ab = a.attr + B.vertex_offset[r.img] * K;
+    const float* a0 = ab + int64_t(it.vid[0]) * K;
+    const float* a1 = ab + int64_t(it.vid[1]) * K;
+    const float* a2 = ab + int64_t(it.vid[2]) * K;
+    for (int k = 0; k < K; k += 4) {
+      const int n = min(4, K - k);
+      const float4 x = load_chunk(a0 + k, n, vec_rows), y = load_chunk(a1 + k, n, vec_rows),
+                   z = load_chunk(a2 + k, n, vec_rows);
+      store_chunk(o + k,
+                  make_float4(lerp3(x.x, y.x, z.x, it.b), lerp3(x.y, y.y, z.y, it.b),
+                              lerp3(x.z, y.z, z.z, it.b), lerp3(x.w, y.w, z.w, it.b)),
+                  n, vec_rows);
+    }
+  } else {
+    for (int k = 0; k < K; k += 4)
+      store_chunk(o + k, make_float4(0.0f, 0.0f, 0.0f, 0.0f), min(4, K - k), vec_rows);
+  }
+  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
+  p.vp[r.e] = make_float4(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.0f), W), 0.5f),
+                          __fmul_rn(__fmul_rn(__fadd_rn(ny, 1.0f), H), 0.5f),
+                          __fmul_rn(__fmul_rn(__fadd_rn(nz, 1.0f), 1.0f), 0.5f), fg);
+}
+
+__global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B) {
+  const PosArgs& p = a.pos;
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= int64_t(p.L) * B.pix_prefix[B.n]) return;
+  const PixelRef r = decode(B, p.L, q);
+  if (__ldg(p.z + r.e) == 1.0f) {
+    if (p.d_bary) {
+      p.d_bary[3 * r.e] = 0.0f;
+      p.d_bary[3 * r.e + 1] = 0.0f;
+      p.d_bary[3 * r.e + 2] = 0.0f;
+    }
+    return;
+  }
+  const Interp it = interpolate_clip(p, B, r.img, r.e);
+  float db[3] = {0.0f, 0.0f, 0.0f};
+  const float4 g = p.dvp ? __ldg(p.dvp + r.e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (g.x != 0.0f || g.y != 0.0f) {
+    // viewport z carries no gradient (it only enters comparisons).
+    const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
+    const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
+    const float cw = it.c.w;
+    const float4 dcl = make_float4(dnx / cw, dny / cw, 0.0f,
+                                   -(dnx * it.c.x + dny * it.c.y) / (cw * cw));
+    float4* dv = p.d_clip + B.vertex_offset[r.img];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float b = it.b[i];
+      atomicAdd(dv + it.vid[i], make_float4(b * dcl.x, b * dcl.y, 0.0f, b * dcl.w));
+      db[i] = it.V[i].x * dcl.x + it.V[i].y * dcl.y + it.V[i].w * dcl.w;
+    }
+  }
+  if (a.d_attr_out) {
+    const int K = a.K;
+    const bool vec_rows = (K & 3) == 0;
+    const float* src = a.d_attr_out + r.e * K;
+    const int64_t aoff = B.vertex_offset[r.img] * K;
+    for (int k = 0; k < K; k += 4) {
+      const int n = min(4, K - k);
+      const float4 ga = load_chunk(src + k, n, vec_rows);
+      if (ga.x == 0.0f && ga.y == 0.0f && ga.z == 0.0f && ga.w == 0.0f) continue;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int64_t row = aoff + int64_t(it.vid[i]) * K + k;
+        const float b = it.b[i];
+        add_chunk(a.d_attr + row, make_float4(b * ga.x, b * ga.y, b * ga.z, b * ga.w), n,
+                  vec_rows);
+        if (p.d_bary) {
+          const float4 av = load_chunk(a.attr + row, n, vec_rows);
+          db[i] += av.x * ga.x + av.y * ga.y + av.z * ga.z + av.w * ga.w;
+        }
+      }
+    }
+  }
+  if (p.d_bary) {
+    p.d_bary[3 * r.e] = db[0];
+    p.d_bary[3 * r.e + 1] = db[1];
+    p.d_bary[3 * r.e + 2] = db[2];
+  }
+}
+
 // -------------------------------------------------------------------- splat
 struct SplatArgs {
   const float4* vp;  // [L*P] viewport xyz + foreground flag
   const float* colors;
-  int L, TY;
+  int L;
+  int64_t P;     // pixels covered by the call: plane stride of `saved`
   float coef;
   float* out;
-  float* saved;  // [P, 3, C+1] accumulators (forward output, backward input)
+  float* saved;  // [3 (C+1), P] planar accumulators (forward out, backward in)
   float* accum;
   float* normalized;
   const float* d_out;
@@ -141,10 +297,25 @@ struct SplatArgs {
   float4* d_vp;
 };
 
+// A block covers a kTX x kTY tile of pixels, one per thread; the samples it
+// reads are the tile plus a 1-pixel halo: kRS x (kTY + 2) per layer.
+constexpr int kRS = kTX + 2;
+constexpr int kRR = kRS * (kTY + 2);
+
+// Colors travel through shared memory as float4 groups, zero padded to a
+// multiple of 4 channels, so that one 128-bit load fetches four channels.
+template <int C>
+struct Groups {
+  static constexpr int Q = (C + 3) / 4;
+};
+
 // Separable tap weights of a sample (splat.py:106-115): tap (u, v) weighs
 // ex[u+1] * ey[v+1] with ex = fg * coef * exp(-2 dx^2), ey = exp(-2 dy^2),
 // dx = floor(x) + 0.5 - x + u. Equal to the reference's
-// fg * coef * exp(-2 (dx^2 + dy^2)) up to float rounding.
+// fg * coef * exp(-2 (dx^2 + dy^2)) up to float rounding: the fast
+// exponential's relative error is below 1e-6 for these arguments
+// (|2 dx^2| <= 4.5), well inside the path's 1e-5 tolerance. The forward and
+// the VJP use this same function, so they see identical weights.
 struct Taps {
   float ex[3], ey[3];
   float d0, d1;
@@ -158,33 +329,10 @@ __device__ __forceinline__ Taps taps_of(float4 q, float coef) {
 #pragma unroll
   for (int u = 0; u < 3; ++u) {
     const float dx = __fadd_rn(t.d0, float(u - 1)), dy = __fadd_rn(t.d1, float(u - 1));
-    t.ex[u] = q.w != 0.0f ? __fmul_rn(fc, expf(__fmul_rn(-2.0f, __fmul_rn(dx, dx)))) : 0.0f;
-    t.ey[u] = q.w != 0.0f ? expf(__fmul_rn(-2.0f, __fmul_rn(dy, dy))) : 0.0f;
+    t.ex[u] = q.w != 0.0f ? __fmul_rn(fc, __expf(__fmul_rn(-2.0f, __fmul_rn(dx, dx)))) : 0.0f;
+    t.ey[u] = q.w != 0.0f ? __expf(__fmul_rn(-2.0f, __fmul_rn(dy, dy))) : 0.0f;
   }
   return t;
-}
-
-// Shared-memory region of R samples per layer, row stride `stride`:
-//   z[l*R + i], wx[(l*3 + u+1)*R + i], wy[(l*3 + v+1)*R + i],
-//   col[(l*C + c)*R + i]; every array indexed by i so warps read
-// consecutive words.
-struct Region {
-  float* z;
-  float* wx;
-  float* wy;
-  float* col;
-  int R, stride;
-};
-
-__device__ __forceinline__ Region region_at(float* base, int L, int R, int stride) {
-  Region r;
-  r.R = R;
-  r.stride = stride;
-  r.z = base;
-  r.wx = r.z + L * R;
-  r.wy = r.wx + 3 * L * R;
-  r.col = r.wy + 3 * L * R;
-  return r;
 }
 
 template <int C>
@@ -213,94 +361,56 @@ __device__ __forceinline__ void store_row(float* p, const float* v) {
   }
 }
 
+// A color row as zero-padded float4 groups.
+template <int C>
+__device__ __forceinline__ void load_groups(const float* p, float4* g) {
+  constexpr int Q = Groups<C>::Q;
+  float v[4 * Q];
+#pragma unroll
+  for (int c = C; c < 4 * Q; ++c) v[c] = 0.0f;
+  load_row<C>(p, v);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) g[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
 struct TileRef {
   int img, x0, y0;
 };
 
-__device__ __forceinline__ TileRef tile_of(const Batch& B, int TY) {
+__device__ __forceinline__ TileRef tile_of(const Batch& B) {
   TileRef t;
   const int item = blockIdx.x;
   t.img = find_segment(B.tile_start, B.n, item);
   const int local = item - B.tile_start[t.img];
   const int ntx = B.tiles_x[t.img];
   t.x0 = (local % ntx) * kTX;
-  t.y0 = (local / ntx) * TY;
+  t.y0 = (local / ntx) * kTY;
   return t;
-}
-
-// Loads samples of the region with image origin (x0, y0), all layers.
-// Samples outside the image have fg = 0 (no weight).
-template <int C>
-__device__ void load_region(const SplatArgs& a, const Batch& B, int img, int x0, int y0,
-                            Region r) {
-  const int W = B.width[img], H = B.height[img];
-  const int64_t HW = int64_t(W) * H;
-  const int64_t base = int64_t(a.L) * B.pix_off[img];
-  const int n = a.L * r.R;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int l = k / r.R, i = k - l * r.R;
-    const int y = y0 + i / r.stride, x = x0 + i % r.stride;
-    float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-    float col[C];
-#pragma unroll
-    for (int c = 0; c < C; ++c) col[c] = 0.0f;
-    if (x >= 0 && y >= 0 && x < W && y < H) {
-      const int64_t e = base + l * HW + int64_t(y) * W + x;
-      q = __ldg(a.vp + e);
-      load_row<C>(a.colors + e * C, col);
-    }
-    const Taps t = taps_of(q, a.coef);
-    r.z[l * r.R + i] = q.z;
-#pragma unroll
-    for (int u = 0; u < 3; ++u) {
-      r.wx[(l * 3 + u) * r.R + i] = t.ex[u];
-      r.wy[(l * 3 + u) * r.R + i] = t.ey[u];
-    }
-#pragma unroll
-    for (int c = 0; c < C; ++c) r.col[(l * C + c) * r.R + i] = col[c];
-  }
 }
 
 // Surface index of the splat from sample s reaching pixel p
 // (splat.py:131-145): c = argmin_k |zS_k - zD_0|, t = argmin_k |zD_k - zS_0|
 // (first index on ties); -t if the tap match is strictly better, else c.
-__device__ __forceinline__ int surface_index(const float* z, int R, int s, int p, int L) {
+// z holds every layer's depth, layer k at z[k * kRR + i].
+__device__ __forceinline__ int surface_index(const float* z, int s, int p, int L) {
   const float zD0 = z[p], zS0 = z[s];
   float minc = fabsf(__fsub_rn(zS0, zD0));
   float mint = minc;
   int c = 0, t = 0;
   for (int k = 1; k < L; ++k) {
-    const float dc = fabsf(__fsub_rn(z[k * R + s], zD0));
+    const float dc = fabsf(__fsub_rn(z[k * kRR + s], zD0));
     if (dc < minc) { minc = dc; c = k; }
-    const float dt = fabsf(__fsub_rn(z[k * R + p], zS0));
+    const float dt = fabsf(__fsub_rn(z[k * kRR + p], zS0));
     if (dt < mint) { mint = dt; t = k; }
   }
   return mint < minc ? -t : c;
 }
 
-// normalization_scales = 1 / (max(W - 1, 0) + 1)   (splat.py:168-169)
-__device__ __forceinline__ float norm_scale(float w) {
-  return __fdiv_rn(1.0f, __fadd_rn(fmaxf(__fsub_rn(w, 1.0f), 0.0f), 1.0f));
-}
-
-template <int C>
-__global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
-  extern __shared__ __align__(16) float smem[];
-  const TileRef tr = tile_of(B, a.TY);
-  const int TY = a.TY, L = a.L;
-  const int stride = kTX + 2, R = stride * (TY + 2);
-  const Region r = region_at(smem, L, R, stride);
-  load_region<C>(a, B, tr.img, tr.x0 - 1, tr.y0 - 1, r);
-  __syncthreads();
-
-  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
-  const int W = B.width[tr.img], H = B.height[tr.img];
-  const int px = tr.x0 + tx, py = tr.y0 + ty;
-  if (px >= W || py >= H) return;
-  const int p = (ty + 1) * stride + tx + 1;
-
-  // Surface index of each of the 9 taps reaching p (independent of layer).
-  int surf[9];
+// Surface indexes of the 9 taps reaching pixel p of the region (0 where the
+// source lies outside the image); bit j of the result marks tap j valid.
+// Tap j = (u + 1) * 3 + (v + 1) comes from the sample at p - (u, v).
+__device__ __forceinline__ unsigned tap_surfaces(const float* z, int p, int px, int py,
+                                                 int W, int H, int L, int surf[9]) {
   unsigned ok = 0;
 #pragma unroll
   for (int j = 0; j < 9; ++j) {
@@ -308,43 +418,123 @@ __global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
     const int sx = px - u, sy = py - v;
     const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
     ok |= unsigned(in) << j;
-    surf[j] = in ? surface_index(r.z, R, p - v * stride - u, p, L) : 0;
+    surf[j] = in ? surface_index(z, p - v * kRS - u, p, L) : 0;
   }
-  // Accumulate in the reference's order (layer, u, v); class 0 = in front
-  // of the surface, 1 = at it, 2 = behind it.
-  float acc[3][C], wacc[3] = {0.0f, 0.0f, 0.0f};
+  return ok;
+}
+
+// normalization_scales = 1 / (max(W - 1, 0) + 1)   (splat.py:168-169);
+// __frcp_rn is the correctly rounded reciprocal, the same value as the
+// division.
+__device__ __forceinline__ float norm_scale(float w) {
+  return __frcp_rn(__fadd_rn(fmaxf(__fsub_rn(w, 1.0f), 0.0f), 1.0f));
+}
+
+// acc += w * color over the float4 groups, two channels per packed f32x2 FMA.
+template <int Q>
+__device__ __forceinline__ void accumulate(float2 (&acc)[2 * Q], float& wacc, const float4* c,
+                                           float w) {
+  const float2 w2 = make_float2(w, w);
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+  for (int q = 0; q < Q; ++q) {
+    acc[2 * q] = __ffma2_rn(w2, make_float2(c[q].x, c[q].y), acc[2 * q]);
+    acc[2 * q + 1] = __ffma2_rn(w2, make_float2(c[q].z, c[q].w), acc[2 * q + 1]);
+  }
+  wacc = __fadd_rn(wacc, w);
+}
+
+// Forward: per layer and halo sample the depth, the separable tap weights
+// and the color go to shared memory,
+//   z[l][i], wx[l][u][i], wy[l][v][i] (floats), col[l][q][i] (float4),
+// every array indexed by the region sample i so that a warp reads
+// consecutive words; then each pixel gathers the 9 taps of every layer with
+// the per-tap surface test, normalizes, composites and stores.
+template <int C>
+__global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
+  constexpr int Q = Groups<C>::Q;
+  extern __shared__ __align__(16) float smem[];
+  const TileRef tr = tile_of(B);
+  const int L = a.L;
+  float* zs = smem;
+  float* wx = zs + L * kRR;
+  float* wy = wx + 3 * L * kRR;
+  float4* col = reinterpret_cast<float4*>(wy + 3 * L * kRR);
+  const int W = B.width[tr.img], H = B.height[tr.img];
+  {
+    const int64_t HW = int64_t(W) * H;
+    const int64_t base = int64_t(L) * B.pix_off[tr.img];
+    for (int k = threadIdx.x; k < L * kRR; k += blockDim.x) {
+      const int l = k / kRR, i = k - l * kRR;
+      const int ry = i / kRS;
+      const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
+      float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+      float4 c[Q];
 #pragma unroll
-    for (int c = 0; c < C; ++c) acc[k][c] = 0.0f;
+      for (int g = 0; g < Q; ++g) c[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (x >= 0 && y >= 0 && x < W && y < H) {
+        const int64_t e = base + l * HW + int64_t(y) * W + x;
+        q = __ldg(a.vp + e);
+        // A background sample weighs 0 everywhere: its color is not read.
+        if (q.w != 0.0f) load_groups<C>(a.colors + e * C, c);
+      }
+      const Taps t = taps_of(q, a.coef);
+      zs[k] = q.z;
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        wx[(l * 3 + u) * kRR + i] = t.ex[u];
+        wy[(l * 3 + u) * kRR + i] = t.ey[u];
+      }
+#pragma unroll
+      for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + i] = c[g];
+    }
+  }
+  __syncthreads();
+
+  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+  const int px = tr.x0 + tx, py = tr.y0 + ty;
+  if (px >= W || py >= H) return;
+  const int p = (ty + 1) * kRS + tx + 1;
+  int surf[9];
+  const unsigned ok = tap_surfaces(zs, p, px, py, W, H, L, surf);
+
+  // Class 0 = in front of the surface, 1 = at it, 2 = behind it
+  // (splat.py:149-162), accumulated layer by layer.
+  float2 acc0[2 * Q], acc1[2 * Q], acc2[2 * Q];
+  float wacc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int h = 0; h < 2 * Q; ++h) {
+    acc0[h] = make_float2(0.0f, 0.0f);
+    acc1[h] = acc0[h];
+    acc2[h] = acc0[h];
+  }
   for (int l = 0; l < L; ++l) {
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       if (!((ok >> j) & 1)) continue;
       const int u = j / 3 - 1, v = j % 3 - 1;
-      const int s = p - v * stride - u;
-      const float wxv = r.wx[(l * 3 + u + 1) * R + s];
+      const int s = p - v * kRS - u;
+      const float wxv = wx[(l * 3 + u + 1) * kRR + s];
       if (wxv == 0.0f) continue;
-      const float w = __fmul_rn(wxv, r.wy[(l * 3 + v + 1) * R + s]);
-      float t[C];
+      const float w = __fmul_rn(wxv, wy[(l * 3 + v + 1) * kRR + s]);
+      float4 c[Q];
 #pragma unroll
-      for (int c = 0; c < C; ++c) t[c] = __fmul_rn(w, r.col[(l * C + c) * R + s]);
-      if (surf[j] > l) {
-#pragma unroll
-        for (int c = 0; c < C; ++c) acc[0][c] = __fadd_rn(acc[0][c], t[c]);
-        wacc[0] = __fadd_rn(wacc[0], w);
-      } else if (surf[j] == l) {
-#pragma unroll
-        for (int c = 0; c < C; ++c) acc[1][c] = __fadd_rn(acc[1][c], t[c]);
-        wacc[1] = __fadd_rn(wacc[1], w);
-      } else {
-#pragma unroll
-        for (int c = 0; c < C; ++c) acc[2][c] = __fadd_rn(acc[2][c], t[c]);
-        wacc[2] = __fadd_rn(wacc[2], w);
-      }
+      for (int g = 0; g < Q; ++g) c[g] = col[(l * Q + g) * kRR + s];
+      if (surf[j] > l)
+        accumulate<Q>(acc0, wacc[0], c, w);
+      else if (surf[j] == l)
+        accumulate<Q>(acc1, wacc[1], c, w);
+      else
+        accumulate<Q>(acc2, wacc[2], c, w);
     }
   }
 
+  float acc[3][4 * Q];
+#pragma unroll
+  for (int h = 0; h < 2 * Q; ++h) {
+    acc[0][2 * h] = acc0[h].x; acc[0][2 * h + 1] = acc0[h].y;
+    acc[1][2 * h] = acc1[h].x; acc[1][2 * h + 1] = acc1[h].y;
+    acc[2][2 * h] = acc2[h].x; acc[2][2 * h + 1] = acc2[h].y;
+  }
   float n[3][C];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -363,12 +553,11 @@ __global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
   }
   store_row<C>(a.out + pix * C, o);
   if (a.saved) {
-    float* sv = a.saved + pix * (3 * (C + 1));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) sv[k * (C + 1) + c] = acc[k][c];
-      sv[k * (C + 1) + C] = wacc[k];
+      for (int c = 0; c < C; ++c) a.saved[(k * (C + 1) + c) * a.P + pix] = acc[k][c];
+      a.saved[(k * (C + 1) + C) * a.P + pix] = wacc[k];
     }
   }
   if (a.accum || a.normalized) {
@@ -424,37 +613,42 @@ __device__ __forceinline__ void accum_adjoint(const float acc[3][C], const float
   }
 }
 
+// Backward, gather form: the adjoints of the saved accumulators of the tile
+// plus a 1-pixel ring go to shared memory, g[k][q][i] (float4 groups of the
+// color adjoint of class k) and h[k][i] (weight adjoint), next to every
+// layer's depth z[l][i]; each sample of the tile then reads those of the 9
+// pixels it reached, in the class its surface test picked, and writes
+// d color and d viewport xy. No atomics.
 template <int C>
-__global__ void __launch_bounds__(256) splat_bwd_kernel(SplatArgs a, Batch B) {
+__global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B) {
+  constexpr int Q = Groups<C>::Q;
   extern __shared__ __align__(16) float smem[];
-  const TileRef tr = tile_of(B, a.TY);
-  const int TY = a.TY, L = a.L;
+  const TileRef tr = tile_of(B);
+  const int L = a.L;
   const int W = B.width[tr.img], H = B.height[tr.img];
   const int64_t HW = int64_t(W) * H;
-  // Tile + 1-pixel ring: every layer's depth (for the surface tests) and the
-  // adjoints of the accumulators, [3*(C+1)][R1] (g[k][c], then h[k]).
-  const int S1 = kTX + 2, R1 = S1 * (TY + 2);
   float* zs = smem;
-  float* adj = zs + L * R1;
+  float4* gs = reinterpret_cast<float4*>(zs + L * kRR);
+  float* hs = reinterpret_cast<float*>(gs + 3 * Q * kRR);
   const int64_t lbase = int64_t(L) * B.pix_off[tr.img];
-  for (int i = threadIdx.x; i < R1; i += blockDim.x) {
-    const int qx = tr.x0 - 1 + i % S1, qy = tr.y0 - 1 + i / S1;
+  for (int i = threadIdx.x; i < kRR; i += blockDim.x) {
+    const int ry = i / kRS;
+    const int qx = tr.x0 - 1 + (i - ry * kRS), qy = tr.y0 - 1 + ry;
     float g[3][C], h[3];
     if (qx >= 0 && qy >= 0 && qx < W && qy < H) {
       const int64_t pix = B.pix_off[tr.img] + int64_t(qy) * W + qx;
-      const float* sv = a.saved + pix * (3 * (C + 1));
       float acc[3][C], wacc[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
 #pragma unroll
-        for (int c = 0; c < C; ++c) acc[k][c] = __ldg(sv + k * (C + 1) + c);
-        wacc[k] = __ldg(sv + k * (C + 1) + C);
+        for (int c = 0; c < C; ++c) acc[k][c] = __ldg(a.saved + (k * (C + 1) + c) * a.P + pix);
+        wacc[k] = __ldg(a.saved + (k * (C + 1) + C) * a.P + pix);
       }
       float d[C];
       load_row<C>(a.d_out + pix * C, d);
       accum_adjoint<C>(acc, wacc, d, g, h);
       for (int l = 0; l < L; ++l)
-        zs[l * R1 + i] = __ldg(&a.vp[lbase + l * HW + int64_t(qy) * W + qx].z);
+        zs[l * kRR + i] = __ldg(&a.vp[lbase + l * HW + int64_t(qy) * W + qx].z);
     } else {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -462,21 +656,26 @@ __global__ void __launch_bounds__(256) splat_bwd_kernel(SplatArgs a, Batch B) {
 #pragma unroll
         for (int c = 0; c < C; ++c) g[k][c] = 0.0f;
       }
-      for (int l = 0; l < L; ++l) zs[l * R1 + i] = 1.0f;
+      for (int l = 0; l < L; ++l) zs[l * kRR + i] = 1.0f;
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      float v[4 * Q];
 #pragma unroll
-      for (int c = 0; c < C; ++c) adj[(k * (C + 1) + c) * R1 + i] = g[k][c];
-      adj[(k * (C + 1) + C) * R1 + i] = h[k];
+      for (int c = 0; c < 4 * Q; ++c) v[c] = c < C ? g[k][c] : 0.0f;
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+        gs[(k * Q + q) * kRR + i] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      hs[k * kRR + i] = h[k];
     }
   }
   __syncthreads();
-
   const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
   const int sx = tr.x0 + tx, sy = tr.y0 + ty;
   if (sx >= W || sy >= H) return;
-  const int s1 = (ty + 1) * S1 + tx + 1;  // this sample's pixel in the ring grid
+  const int s1 = (ty + 1) * kRS + tx + 1;  // this sample's pixel in the ring grid
+  // Surface index of this sample's splat at each of the 9 pixels it reaches:
+  // pixel s1 + (u, v) sees this sample as its tap (u, v).
   int surf[9];
   unsigned ok = 0;
 #pragma unroll
@@ -485,41 +684,51 @@ __global__ void __launch_bounds__(256) splat_bwd_kernel(SplatArgs a, Batch B) {
     const int px = sx + u, py = sy + v;
     const bool in = px >= 0 && py >= 0 && px < W && py < H;
     ok |= unsigned(in) << j;
-    surf[j] = in ? surface_index(zs, R1, s1, s1 + v * S1 + u, L) : 0;
+    surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
   }
   const int64_t ebase = lbase + int64_t(sy) * W + sx;
   for (int l = 0; l < L; ++l) {
     const int64_t e = ebase + l * HW;
     const float4 q = __ldg(a.vp + e);
-    float dcol[C];
+    float2 dcol[2 * Q];
 #pragma unroll
-    for (int c = 0; c < C; ++c) dcol[c] = 0.0f;
+    for (int hh = 0; hh < 2 * Q; ++hh) dcol[hh] = make_float2(0.0f, 0.0f);
     float dvx = 0.0f, dvy = 0.0f;
     if (q.w != 0.0f) {
       const Taps t = taps_of(q, a.coef);
-      float col[C];
-      load_row<C>(a.colors + e * C, col);
+      float4 col[Q];
+      load_groups<C>(a.colors + e * C, col);
 #pragma unroll
       for (int j = 0; j < 9; ++j) {
         if (!((ok >> j) & 1)) continue;
         const int u = j / 3 - 1, v = j % 3 - 1;
         const float w = __fmul_rn(t.ex[u + 1], t.ey[v + 1]);
         const int k = surf[j] > l ? 0 : (surf[j] == l ? 1 : 2);
-        const float* ak = adj + k * (C + 1) * R1 + s1 + v * S1 + u;
-        float dw = ak[C * R1];
+        const int at = s1 + v * kRS + u;
+        const float4* gk = gs + k * Q * kRR + at;
+        float dw = hs[k * kRR + at];
+        const float2 w2 = make_float2(w, w);
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-          const float gc = ak[c * R1];
-          dcol[c] += w * gc;
-          dw += gc * col[c];
+        for (int g = 0; g < Q; ++g) {
+          const float4 gv = gk[g * kRR];
+          dcol[2 * g] = __ffma2_rn(w2, make_float2(gv.x, gv.y), dcol[2 * g]);
+          dcol[2 * g + 1] = __ffma2_rn(w2, make_float2(gv.z, gv.w), dcol[2 * g + 1]);
+          dw = fmaf(gv.x, col[g].x, fmaf(gv.y, col[g].y,
+                    fmaf(gv.z, col[g].z, fmaf(gv.w, col[g].w, dw))));
         }
         // d w / d (x, y) = 4 w (dx, dy): the floor carries no gradient.
         const float f = 4.0f * w * dw;
-        dvx += f * (t.d0 + float(u));
-        dvy += f * (t.d1 + float(v));
+        dvx = fmaf(f, t.d0 + float(u), dvx);
+        dvy = fmaf(f, t.d1 + float(v), dvy);
       }
     }
-    store_row<C>(a.d_colors + e * C, dcol);
+    float dc[4 * Q];
+#pragma unroll
+    for (int hh = 0; hh < 2 * Q; ++hh) {
+      dc[2 * hh] = dcol[hh].x;
+      dc[2 * hh + 1] = dcol[hh].y;
+    }
+    store_row<C>(a.d_colors + e * C, dc);
     a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
   }
 }
@@ -533,15 +742,17 @@ float gaussian_coef() {
   return float((1.0 + 0.05) / sum);
 }
 
-size_t fwd_smem(int L, int C) { return size_t(L) * (kTX + 2) * (kTY + 2) * 4 * (7 + C); }
+// Shared memory per block: z, 3 + 3 weights and the padded color groups per
+// layer sample (forward); every layer's z, the padded color adjoints and the
+// weight adjoint of the 3 classes per ring pixel (backward).
+size_t fwd_smem(int L, int C) { return size_t(L) * kRR * 4 * (7 + 4 * ((C + 3) / 4)); }
 size_t bwd_smem(int L, int C) {
-  return size_t(L + 3 * (C + 1)) * (kTX + 2) * (kTY + 2) * 4;
+  return size_t(L + 3 * 4 * ((C + 3) / 4) + 3) * kRR * 4;
 }
 
 template <int C>
 int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
               cudaStream_t stream, std::string& err) {
-  a.TY = kTY;
   const size_t smem = bwd ? bwd_smem(a.L, C) : fwd_smem(a.L, C);
   auto kern = bwd ? splat_bwd_kernel<C> : splat_fwd_kernel<C>;
   // Raise the dynamic shared-memory limit once per kernel and size (host-side
@@ -588,6 +799,15 @@ bool aligned16(std::initializer_list<const void*> ptrs) {
   return true;
 }
 
+// Pixels spanned by the images of one call: the plane stride of the saved
+// accumulators.
+int64_t call_pixels(const dr_image_desc* images, int n) {
+  int64_t P = 0;
+  for (int i = 0; i < n; ++i)
+    P = std::max(P, images[i].pixel_offset + int64_t(images[i].width) * images[i].height);
+  return P;
+}
+
 bool check_batch(int L, int n, const dr_image_desc* images, std::string& err, int& rc) {
   rc = DR_OK;
   if (n < 0 || (n > 0 && !images)) { err = "invalid image table"; rc = DR_ERR_INVALID_ARGUMENT; return false; }
@@ -609,6 +829,72 @@ int run_positions(K kern, const PosArgs& a, const dr_image_desc* images, int n, 
 }
 
 }  // namespace
+
+int samples_fwd_launch(const float* attributes, int K, const float* clip,
+                       const int32_t* tris, const int32_t* ids, const float* z,
+                       const float* bary, const dr_image_desc* images, int n, int L,
+                       float* attr_out, float* positions, cudaStream_t stream,
+                       std::string& err) {
+  int rc;
+  if (!check_batch(L, n, images, err, rc)) return rc;
+  if (K < 1 || K > DR_MAX_CHANNELS) { err = "channels must be in [1, 16]"; return DR_ERR_INVALID_ARGUMENT; }
+  if (!aligned16({clip, positions}) ||
+      (K % 4 == 0 && !aligned16({attributes, attr_out}))) {
+    err = "clip_vertices, positions (and, with a multiple of 4 channels, the attribute "
+          "buffers) must be 16-byte aligned";
+    return DR_ERR_MISALIGNED;
+  }
+  SampleArgs a{};
+  a.pos.clip = reinterpret_cast<const float4*>(clip);
+  a.pos.tris = tris; a.pos.ids = ids; a.pos.z = z; a.pos.bary = bary; a.pos.L = L;
+  a.pos.vp = reinterpret_cast<float4*>(positions);
+  a.attr = attributes; a.K = K; a.attr_out = attr_out;
+  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+    Batch b;
+    if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
+    const int64_t total = int64_t(L) * b.pix_prefix[cnt];
+    if (total > 0) samples_fwd_kernel<<<unsigned((total + 255) / 256), 256, 0, stream>>>(a, b);
+  }
+  return launch_status("interpolate + splat positions", err);
+}
+
+int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
+                       const float* attributes, int K, const float* clip,
+                       const int32_t* tris, const int32_t* ids, const float* z,
+                       const float* bary, const dr_image_desc* images, int n, int L,
+                       float* d_attributes, float* d_clip, float* d_bary,
+                       cudaStream_t stream, std::string& err) {
+  int rc;
+  if (!check_batch(L, n, images, err, rc)) return rc;
+  if (K < 1 || K > DR_MAX_CHANNELS) { err = "channels must be in [1, 16]"; return DR_ERR_INVALID_ARGUMENT; }
+  if (!d_clip || (d_attr_out && !d_attributes)) {
+    err = "d_clip_vertices (and d_attributes with d_attr_out) must be non-null";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  if (!aligned16({d_positions, clip, d_clip}) ||
+      (K % 4 == 0 && !aligned16({d_attr_out, attributes, d_attributes}))) {
+    err = "d_positions, clip_vertices, d_clip_vertices (and, with a multiple of 4 "
+          "channels, the attribute buffers) must be 16-byte aligned";
+    return DR_ERR_MISALIGNED;
+  }
+  SampleArgs a{};
+  a.pos.clip = reinterpret_cast<const float4*>(clip);
+  a.pos.tris = tris; a.pos.ids = ids; a.pos.z = z; a.pos.bary = bary; a.pos.L = L;
+  a.pos.dvp = reinterpret_cast<const float4*>(d_positions);
+  a.pos.d_clip = reinterpret_cast<float4*>(d_clip);
+  a.pos.d_bary = d_bary;
+  a.attr = attributes; a.K = K;
+  a.d_attr_out = d_attr_out; a.d_attr = d_attributes;
+  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+    Batch b;
+    if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
+    const int64_t total = int64_t(L) * b.pix_prefix[cnt];
+    if (total > 0) samples_bwd_kernel<<<unsigned((total + 255) / 256), 256, 0, stream>>>(a, b);
+  }
+  return launch_status("interpolate + splat positions backward", err);
+}
 
 int positions_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
                          const float* z, const float* bary, const dr_image_desc* images,
@@ -663,6 +949,7 @@ int splat_fwd_launch(const float* positions, const float* colors, int C,
   a.vp = reinterpret_cast<const float4*>(positions);
   a.colors = colors;
   a.L = L;
+  a.P = call_pixels(images, n);
   a.coef = gaussian_coef();
   a.out = out; a.saved = saved; a.accum = accum; a.normalized = normalized;
   return dispatch(false, C, a, images, n, stream, err);
@@ -688,6 +975,7 @@ int splat_bwd_launch(const float* d_out, const float* positions, const float* co
   a.vp = reinterpret_cast<const float4*>(positions);
   a.colors = colors;
   a.L = L;
+  a.P = call_pixels(images, n);
   a.coef = gaussian_coef();
   a.saved = const_cast<float*>(saved);
   a.d_out = d_out; a.d_colors = d_colors;

@@ -385,6 +385,64 @@ def diff_barycentrics_packed(clip, triangles, ids, z, batch, num_layers):
   return _DiffBary.apply(clip, triangles, ids, z, batch, num_layers)
 
 
+# --------------------------------------- fused attributes + splat positions
+class _Samples(torch.autograd.Function):
+  """interpolate (background 0) and splat positions in one pass per sample."""
+
+  @staticmethod
+  def forward(ctx, attributes, clip, bary, triangles, ids, z, batch, L):
+    lib = _lib.load()
+    K = attributes.shape[1]
+    out = torch.empty(ids.shape[0], K, dtype=torch.float32, device=ids.device)
+    vp = torch.empty(ids.shape[0], 4, dtype=torch.float32, device=ids.device)
+    with _op("samples_fwd", _groups(batch)):
+      rc = lib.dr_interpolate_with_positions_fwd(
+          _p(attributes), K, _p(clip), _p(triangles), _p(ids), _p(z), _p(bary),
+          batch.ptr, batch.n, L, _p(out), _p(vp), _stream(ids.device))
+    _lib.check(rc, "dr_interpolate_with_positions_fwd")
+    ctx.save_for_backward(attributes, clip, bary, triangles, ids, z)
+    ctx.batch, ctx.L = batch, L
+    ctx.set_materialize_grads(False)
+    return out, vp
+
+  @staticmethod
+  def backward(ctx, d_out, d_vp):
+    attributes, clip, bary, triangles, ids, z = ctx.saved_tensors
+    lib = _lib.load()
+    none = (None,) * 6
+    if d_out is None and d_vp is None:
+      return (None, None, None) + none[:5]
+    if d_out is not None:
+      d_out = d_out.contiguous()
+    if d_vp is not None:
+      d_vp = d_vp.contiguous()
+      if d_vp.data_ptr() % 16:
+        d_vp = d_vp.clone()
+    d_attr = torch.zeros_like(attributes)
+    d_clip = torch.zeros_like(clip)
+    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[2] else None
+    with _op("samples_bwd", _groups(ctx.batch)):
+      rc = lib.dr_interpolate_with_positions_bwd(
+          _p(d_out), _p(d_vp), _p(attributes), attributes.shape[1], _p(clip),
+          _p(triangles), _p(ids), _p(z), _p(bary), ctx.batch.ptr, ctx.batch.n, ctx.L,
+          _p(d_attr), _p(d_clip), _p(d_bary), _stream(clip.device))
+    _lib.check(rc, "dr_interpolate_with_positions_bwd")
+    return (d_attr if ctx.needs_input_grad[0] else None,
+            d_clip if ctx.needs_input_grad[1] else None,
+            d_bary, None, None, None, None, None)
+
+
+def interpolate_with_positions_packed(attributes, clip, bary, triangles, ids, z, batch,
+                                      num_layers):
+  """(interpolated attributes [L*P, K] with background 0, splat positions
+  [L*P, 4]) of a packed batch, in one pass when K <= 16."""
+  attributes = _f32(attributes)
+  if attributes.shape[1] > _lib.DR_MAX_CHANNELS:
+    return (interpolate_packed(attributes, bary, triangles, ids, z, batch, num_layers),
+            splat_positions_packed(clip, bary, triangles, ids, z, batch, num_layers))
+  return _Samples.apply(attributes, clip, bary, triangles, ids, z, batch, num_layers)
+
+
 # ------------------------------------------------------------------ splat
 class _Positions(torch.autograd.Function):
   """Viewport xyz + foreground flag of every layer sample (splat.py:207-221)."""
@@ -436,7 +494,7 @@ class _Splat(torch.autograd.Function):
     P = batch.total_pixels
     out = torch.empty(P, C, dtype=torch.float32, device=dev)
     needs_grad = positions.requires_grad or colors.requires_grad
-    saved = (torch.empty(P, 3 * (C + 1), dtype=torch.float32, device=dev)
+    saved = (torch.empty(3 * (C + 1), P, dtype=torch.float32, device=dev)
              if needs_grad else None)
     accum = norm = None
     if want_accum:

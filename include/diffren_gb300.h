@@ -246,13 +246,37 @@ int dr_splat_positions_bwd(const float* d_positions, const float* clip_vertices,
                            int32_t num_layers, float* d_clip_vertices,
                            float* d_barycentrics, void* stream);
 
+/* Fused dr_interpolate_fwd (background 0) and dr_splat_positions_fwd: one
+ * pass over the layer samples writes attributes_out [L, H, W, K] and
+ * positions [L, H, W, 4] with the same bits as the two separate calls. */
+int dr_interpolate_with_positions_fwd(const float* attributes, int32_t num_channels,
+                                      const float* clip_vertices, const int32_t* triangles,
+                                      const int32_t* triangle_ids, const float* z_buffer,
+                                      const float* barycentrics, const dr_image_desc* images,
+                                      int32_t num_images, int32_t num_layers,
+                                      float* attributes_out, float* positions, void* stream);
+
+/* Its VJP: from d_attributes_out (nullable) and d_positions, accumulates
+ * d_attributes [V, K] and d_clip_vertices [V, 4] (caller zeroes both) and
+ * writes d_barycentrics when non-null. */
+int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
+                                      const float* d_positions, const float* attributes,
+                                      int32_t num_channels, const float* clip_vertices,
+                                      const int32_t* triangles, const int32_t* triangle_ids,
+                                      const float* z_buffer, const float* barycentrics,
+                                      const dr_image_desc* images, int32_t num_images,
+                                      int32_t num_layers, float* d_attributes,
+                                      float* d_clip_vertices, float* d_barycentrics,
+                                      void* stream);
+
 /* splat_at_pixel_centers + composite.over (splat.py:26-175,
  * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the
  * per-tap surface test, normalization and back-to-front over compositing.
  * positions [L, H, W, 4] (viewport xyz, fg); colors [L, H, W, C]
  * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
- * saved [H, W, 3, C + 1] receives the fg/surface/bg accumulators and
- * weights the VJP needs (nullable); accum and normalized [3, H, W, C] are
+ * saved [3, C + 1, P] receives the fg/surface/bg accumulators and weights
+ * the VJP needs, one plane of P pixels per value, P = the largest
+ * pixel_offset + width * height of the images (nullable); accum and normalized [3, H, W, C] are
  * the reference's debugging buffers (nullable). With C % 4 == 0 the color
  * and output buffers must be 16-byte aligned. */
 int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,

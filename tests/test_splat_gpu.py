@@ -157,6 +157,50 @@ def test_splat_positions_match_oracle(device):
   np.testing.assert_array_equal(vp[..., 3].cpu().numpy(), (z != 1).astype(np.float32))
 
 
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_interpolate_with_positions_matches_oracle(case, device):
+  """The fused pass equals interpolate + viewport_xyz bit for bit, and its
+  VJP matches float64 autograd of the restatement."""
+  kind, w, h, layers, C = CASES[case]
+  clip, tris, ids, z, b, _, m = scene(kind, w, h, layers, C, case)
+  attr = np.concatenate([m.colors, m.vertices], axis=1)[:, :C + 2]
+  ref_attr = np_splat.interpolate(attr, ids, z, b, tris)
+  ref_xyz = np_splat.viewport_xyz(clip, ids, z, b, tris, w, h)
+  a, c, t, i, zz, bb = to_dev(device, attr, clip, tris, ids.reshape(-1), z.reshape(-1),
+                              b.reshape(-1, 3))
+  a.requires_grad_(True)
+  c.requires_grad_(True)
+  bb.requires_grad_(True)
+  batch = kernels.ImageBatch.single(w, h, len(attr), len(tris))
+  out, vp = kernels.interpolate_with_positions_packed(a, c, bb, t, i, zz, batch, layers)
+  np.testing.assert_array_equal(out.detach().view(layers, h, w, -1).cpu().numpy(), ref_attr)
+  np.testing.assert_array_equal(vp.detach()[:, :3].view(layers, h, w, 3).cpu().numpy(),
+                                ref_xyz)
+  np.testing.assert_array_equal(vp.detach()[:, 3].view(layers, h, w).cpu().numpy(),
+                                (z != 1).astype(np.float32))
+
+  rng = np.random.default_rng(case + 7)
+  ga = rng.standard_normal((layers, h, w, attr.shape[1])).astype(np.float32)
+  gp = rng.standard_normal((layers, h, w, 4)).astype(np.float32)
+  ta = torch.tensor(attr, dtype=torch.float64, requires_grad=True)
+  tc = torch.tensor(clip, dtype=torch.float64, requires_grad=True)
+  tb = torch.tensor(b, dtype=torch.float64, requires_grad=True)
+  ti, tz, tt = torch.tensor(ids), torch.tensor(z), torch.tensor(tris)
+  ro = torch_ref.interpolate(ta, ti, tz, tb, tt)
+  rx = torch_ref.viewport_xyz(tc, ti, tz, tb, tt, w, h)
+  # The viewport z and the foreground flag carry no gradient.
+  loss = (ro * torch.tensor(ga, dtype=torch.float64)).sum() + \
+      (rx[..., :2] * torch.tensor(gp[..., :2], dtype=torch.float64)).sum()
+  ra, rc, rb = torch.autograd.grad(loss, (ta, tc, tb))
+  da, dc, db = torch.autograd.grad(
+      (out, vp), (a, c, bb),
+      (torch.as_tensor(ga, device=device).view(out.shape),
+       torch.as_tensor(gp, device=device).view(vp.shape)))
+  assert_grad_close(da.cpu().numpy(), ra.numpy())
+  assert_grad_close(dc.cpu().numpy(), rc.numpy())
+  assert_grad_close(db.view(layers, h, w, 3).cpu().numpy(), rb.numpy())
+
+
 @pytest.mark.parametrize("C", [4, 3])
 def test_splat_at_pixel_centers_off_center_positions(C, device):
   """The public splat_at_pixel_centers on samples that sit off the pixel
