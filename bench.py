@@ -92,6 +92,7 @@ class Workload:
     self.num_layers = 3
     self.pixels = int(sum(w * h for w, h in sizes))
     self.triangles = int(sum(len(m.triangles) for m in meshes))
+    self.vertices = int(sum(len(m.vertices) for m in meshes))
     rng = np.random.default_rng(seed + 99)
     self.targets = [rng.uniform(0, 1, (h, w, 4)).astype(np.float32) for w, h in sizes]
     for t in self.targets:
@@ -184,32 +185,29 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- our arm
-def kernel_bytes(wl, C=4, K=4):
-  """Algorithmic (compulsory) HBM bytes per launch of each kernel."""
-  L, P = wl.num_layers, wl.pixels
-  T = wl.triangles
+def kernel_bytes(wl, fg, C=4, K=4):
+  """Algorithmic (compulsory) HBM bytes per launch of each kernel: every
+  input read and every output written once. `fg` = foreground layer samples
+  among the L * P; work on background samples stops after their depth."""
+  L, P, T, V = wl.num_layers, wl.pixels, wl.triangles, wl.vertices
+  S = L * P
   return {
-      # indices + 3 gathered clip vertices per triangle, ids + z + bary out
-      "raster": T * (12 + 48) + 20 * L * P,
-      # per layer sample: ids, z, bary in (20 B) + K floats out
-      "interp_fwd": L * P * (20 + 4 * K),
-      # per layer sample: ids, z, bary in; viewport xyz + fg out (16 B)
-      "splat_positions": L * P * (20 + 16),
-      # per layer sample: position (16 B) + color in; per pixel: composited
-      # color and the saved accumulators (3 (C + 1) floats) out
-      "splat_fwd": L * P * (16 + 4 * C) + P * (4 * C + 12 * (C + 1)),
-      # per pixel: saved accumulators + d_out in; per layer sample: position
-      # and color in, d color and d position out
-      "splat_bwd": P * (12 * (C + 1) + 4 * C) + L * P * (16 + 4 * C + 4 * C + 16),
-      # per layer sample: d position, ids, z, bary in (vertex scatter to L2)
-      "splat_positions_bwd": L * P * (16 + 20),
-      # fused interpolation + positions: ids, z, bary in; K floats and the
-      # position out
-      "samples_fwd": L * P * (20 + 4 * K + 16),
-      # its VJP: ids, z, bary, d attribute and d position in
-      "samples_bwd": L * P * (20 + 4 * K + 16),
-      # per layer sample: ids, z, bary, d attribute in
-      "interp_bwd": L * P * (20 + 4 * K),
+      # triangle indices and clip vertices in; ids, z, bary of every sample out
+      "raster": T * 12 + V * 16 + 20 * S,
+      # z of every sample, ids + bary of the foreground ones and the mesh
+      # (indices, clip vertices, attributes) in; K attributes and the
+      # viewport position of every sample out
+      "samples_fwd": 4 * S + 16 * fg + T * 12 + V * (16 + 4 * K) + S * (4 * K + 16),
+      # position of every sample and color of every foreground sample in;
+      # composited color and saved accumulators (3 (C + 1)) per pixel out
+      "splat_fwd": 16 * S + 4 * C * fg + P * (4 * C + 12 * (C + 1)),
+      # saved accumulators and d color per pixel, position of every sample,
+      # color of the foreground ones in; d color and d position per sample out
+      "splat_bwd": P * (12 * (C + 1) + 4 * C) + 16 * S + 4 * C * fg + S * (4 * C + 16),
+      # z of every sample; ids, bary, d position and d attributes of the
+      # foreground ones and the mesh in; vertex gradients (clip + attributes)
+      # read and written once
+      "samples_bwd": 4 * S + fg * (16 + 16 + 4 * K) + T * 12 + V * (16 + 4 * K) * 3,
   }
 
 
@@ -256,6 +254,11 @@ def run_ours(args, rank, world, device):
   step()
   torch.cuda.synchronize(device)
   launches_per_step = kernels.LAUNCHES.count
+  # Foreground layer samples of the workload (for the algorithmic bytes).
+  with torch.no_grad():
+    _, z_fg, _ = r.rasterize(kernels.transform(verts, cams, r.batch))
+    fg = int((z_fg != 1.0).sum())
+  del z_fg
   graph = torch.cuda.CUDAGraph()
   with torch.cuda.graph(graph):
     step()
@@ -314,7 +317,7 @@ def run_ours(args, rank, world, device):
   plain = None
   if not args.no_plain and rank == 0:
     plain = run_plain(wl, device, args)
-  return dict(wl=wl, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
+  return dict(wl=wl, fg=fg, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
               loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
               plain=plain, renderer=r)
 
@@ -463,7 +466,7 @@ def main():
     return
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
-  nbytes = kernel_bytes(wl)
+  nbytes = kernel_bytes(wl, res["fg"])
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
   value = world * wl.pixels / res["ms"] / 1e3
@@ -475,7 +478,8 @@ def main():
       "data": "synthetic (seeded meshes, cameras and targets)",
       "config": {"workload": wl.desc, "num_images": len(wl.meshes),
                  "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
-                 "num_layers": wl.num_layers, "parallelism": "replicas" if world > 1 else "1 GPU",
+                 "num_layers": wl.num_layers,
+                 "foreground_samples": res["fg"], "parallelism": "replicas" if world > 1 else "1 GPU",
                  "l2": "per-step working set of several GB > 129 MB L2",
                  "cuda_graph": True},
       "e2e": {"value": world * wl.pixels / res["ms_e2e"] / 1e3, "unit": "Mpix/s",
@@ -486,6 +490,8 @@ def main():
           "batched_over_plain": value / world / res["plain"]["value"]},
       "gpu_launches": res["launches"] * args.steps,
       "kernels_ms": {k: round(v, 4) for k, v in pk.items()},
+      "kernels_gbs": {k: round(nbytes[k] / (pk[k] * 1e-3) / 1e9, 1)
+                      for k in pk if k in nbytes},
       "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                    "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                    "algorithmic_bytes": nbytes[dom], "traffic": None},

@@ -267,7 +267,16 @@ __device__ __forceinline__ uint32_t discretize_z(float z) {
     sh = 53;
     N = (1ull << 53) - shift_round_even(M, -53 - E);
   }
-  u128 Q = u128(N) * 2147483647u;  // a * S = Q * 2^-sh exactly
+  // a * S = P * 2^-sh exactly, P = N * S < 2^(sh + 32). Rounding P to 53
+  // significant bits moves it by at most 2^(sh - 22) and never below
+  // floor(P / 2^sh) * 2^sh (a multiple of the rounding unit), so the floor
+  // only changes when P's fraction lies within 2^(sh - 22) of the next
+  // integer: otherwise floor(P / 2^sh) is the answer.
+  const uint64_t lo = N * 2147483647ull, hi = __umul64hi(N, 2147483647ull);
+  if (sh < 64 && sh >= 23 &&
+      (lo & ((1ull << sh) - 1)) < (1ull << sh) - (1ull << (sh - 22)))
+    return uint32_t((lo >> sh) | (hi << (64 - sh)));
+  u128 Q = u128(N) * 2147483647u;
   const int bl = bitlen128(Q);
   if (bl > 53) Q = round_bits_even(Q, bl - 53);
   return uint32_t(Q >> sh);

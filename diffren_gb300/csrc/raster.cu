@@ -205,22 +205,26 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B)
     }
 }
 
+// Per chunk of up to kThreads triangles overlapping the tile, compacted to
+// those with at least one candidate pixel (slot = rank among them).
 struct FineSmem {
   long long* m;          // [9][kThreads]
   float* vz;             // [3][kThreads]
   float* vw;             // [3][kThreads]
   int* tid;              // [kThreads] local triangle id
   int* geom;             // [kThreads] x0 | y0 << 8 | width << 16 (tile-local)
-  int* off;              // [kThreads] exclusive candidate offsets
+  int* inv;              // [kThreads] ceil(2^20 / width)
+  int* off;              // [kThreads + 1] exclusive candidate offsets
   long long* pxf;        // [TW] fixed-point pixel-center x
   long long* pyf;        // [TH]
   unsigned long long* keys;  // [L][TW*TH]
+  unsigned char* first;  // [8 * TW*TH] slot holding candidate 32 g, per g
 };
 
 __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
   return size_t(9) * kThreads * 8 + size_t(TW + TH) * 8 +
          size_t(L) * TW * TH * 8 + size_t(6) * kThreads * 4 +
-         size_t(3) * kThreads * 4 + 64;
+         size_t(4) * kThreads * 4 + 16 + size_t(8) * TW * TH + 64;
 }
 
 // Persistent fine rasterizer. Each block takes (image, tile) items from a
@@ -244,7 +248,9 @@ __global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Bat
     s.vw = reinterpret_cast<float*>(p); p += size_t(3) * kThreads * 4;
     s.tid = reinterpret_cast<int*>(p); p += kThreads * 4;
     s.geom = reinterpret_cast<int*>(p); p += kThreads * 4;
-    s.off = reinterpret_cast<int*>(p);
+    s.inv = reinterpret_cast<int*>(p); p += kThreads * 4;
+    s.off = reinterpret_cast<int*>(p); p += (kThreads + 4) * 4;
+    s.first = p;
   }
   const unsigned long long kEmpty = empty_key(a.depth_mode);
   const bool disc = a.depth_mode == DR_DEPTH_DISCRETIZED;
@@ -275,48 +281,72 @@ __global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Bat
 
     for (int c0 = 0; c0 < nsrc; c0 += kThreads) {
       const int i = c0 + threadIdx.x;
-      int cnt = 0;
+      int cnt = 0, g = 0, cx0 = 0, cy0 = 0, cw = 1;
       if (i < nsrc) {
-        const int g = i < nbin ? a.bins[bin0 + i] : a.large_list[tri0 + (i - nbin)];
+        g = i < nbin ? a.bins[bin0 + i] : a.large_list[tri0 + (i - nbin)];
         const int4 box = a.bbox[g];
-        const int cx0 = max(box.x, x0) - x0, cx1 = min(box.y, x0 + tw) - x0;
-        const int cy0 = max(box.z, y0) - y0, cy1 = min(box.w, y0 + th) - y0;
+        cx0 = max(box.x, x0) - x0;
+        cy0 = max(box.z, y0) - y0;
+        const int cx1 = min(box.y, x0 + tw) - x0, cy1 = min(box.w, y0 + th) - y0;
         if (cx1 > cx0 && cy1 > cy0) {
-          cnt = (cx1 - cx0) * (cy1 - cy0);
-          const TriSetup* src = a.setup + g;
-          const int4* q = reinterpret_cast<const int4*>(src);
-          int4 r[6];
-#pragma unroll
-          for (int k = 0; k < 6; ++k) r[k] = __ldg(q + k);
-          const long long* mm = reinterpret_cast<const long long*>(r);
-          const float* ff = reinterpret_cast<const float*>(r) + 18;
-#pragma unroll
-          for (int k = 0; k < 9; ++k) s.m[k * kThreads + threadIdx.x] = mm[k];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            s.vz[k * kThreads + threadIdx.x] = ff[k];
-            s.vw[k * kThreads + threadIdx.x] = ff[3 + k];
-          }
-          s.tid[threadIdx.x] = int(g - tri0);
-          s.geom[threadIdx.x] = cx0 | (cy0 << 8) | ((cx1 - cx0) << 16);
+          cw = cx1 - cx0;
+          cnt = cw * (cy1 - cy0);
         }
       }
+      // One scan gives each triangle with candidates its compacted slot
+      // (bits 20+) and its first candidate (bits 0-19): at most
+      // kThreads * 1024 candidates per chunk.
       int excl;
-      const int total = block_exclusive_scan<kThreads>(cnt, s_warp, excl);
-      s.off[threadIdx.x] = excl;
+      const int tot = block_exclusive_scan<kThreads>(cnt | (cnt > 0 ? 1 << 20 : 0), s_warp, excl);
+      const int total = tot & 0xfffff, ntri = tot >> 20;
+      if (cnt > 0) {
+        const int slot = excl >> 20, off = excl & 0xfffff;
+        int4 r[6];
+        const int4* src = reinterpret_cast<const int4*>(a.setup + g);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k] = __ldg(src + k);
+        const long long* mm = reinterpret_cast<const long long*>(r);
+        const float* ff = reinterpret_cast<const float*>(r) + 18;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) s.m[k * kThreads + slot] = mm[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          s.vz[k * kThreads + slot] = ff[k];
+          s.vw[k * kThreads + slot] = ff[3 + k];
+        }
+        s.tid[slot] = int(g - tri0);
+        s.geom[slot] = cx0 | (cy0 << 8) | (cw << 16);
+        s.inv[slot] = ((1 << 20) + cw - 1) / cw;
+        s.off[slot] = off;
+        // This triangle holds candidate 32 q for every q with 32 q in
+        // [off, off + cnt).
+        for (int q = (off + 31) >> 5; (q << 5) < off + cnt; ++q) s.first[q] = (unsigned char)slot;
+      }
+      if (threadIdx.x == 0) s.off[ntri] = total;
       __syncthreads();
 
-      for (int k = threadIdx.x; k < total; k += kThreads) {
-        const int j = find_segment(s.off, kThreads, k);
+      // Warp-wide groups of 32 consecutive candidates. The group's first
+      // candidate lies in triangle j0 = first[q]; the triangles that start
+      // inside the group mark their start positions in one 32-bit mask, and
+      // lane t's triangle is j0 plus the marks at positions 1..t.
+      const int lane = threadIdx.x & 31;
+      for (int q = threadIdx.x >> 5; (q << 5) < total; q += kThreads / 32) {
+        const int base = q << 5;
+        const int j0 = s.first[q];
+        const int jn = j0 + 1 + lane;
+        const int d = jn <= ntri ? s.off[jn] - base : 32;
+        const unsigned starts = __reduce_or_sync(0xffffffffu, d > 0 && d < 32 ? 1u << d : 0u);
+        const int k = base + lane;
+        if (k >= total) continue;
+        const int j = j0 + __popc(starts & ((2u << lane) - 1u));
         const int geom = s.geom[j];
-        const int w = geom >> 16;
-        const int r = k - s.off[j];
-        const int ry = r / w;
-        const int lx = (geom & 255) + (r - ry * w);
+        const int rr = k - s.off[j];
+        const int ry = int((unsigned(rr) * unsigned(s.inv[j])) >> 20);  // rr / width
+        const int lx = (geom & 255) + (rr - ry * (geom >> 16));
         const int ly = ((geom >> 8) & 255) + ry;
         long long m[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) m[q] = s.m[q * kThreads + j];
+        for (int t = 0; t < 9; ++t) m[t] = s.m[t * kThreads + j];
         long long e[3];
         edge_values(m, s.pxf[lx], s.pyf[ly], e);
         if (!inside(e)) continue;

@@ -58,16 +58,33 @@ struct Interp {
   float b[3];
 };
 
+// A layer sample's triangle id and barycentrics, loaded together with its
+// depth so that the three loads overlap.
+struct SampleRef {
+  float z;
+  int id;
+  float b[3];
+};
+
+__device__ __forceinline__ SampleRef load_sample(const PosArgs& a, int64_t e) {
+  SampleRef s;
+  s.z = __ldg(a.z + e);
+  s.id = __ldg(a.ids + e);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) s.b[i] = __ldg(a.bary + 3 * e + i);
+  return s;
+}
+
 __device__ __forceinline__ Interp interpolate_clip(const PosArgs& a, const Batch& B,
-                                                   int img, int64_t e) {
+                                                   int img, const SampleRef& sr) {
   Interp r;
-  const int32_t* t = a.tris + 3 * (B.triangle_offset[img] + __ldg(a.ids + e));
+  const int32_t* t = a.tris + 3 * (B.triangle_offset[img] + sr.id);
   const float4* vb = a.clip + B.vertex_offset[img];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     r.vid[i] = __ldg(t + i);
     r.V[i] = __ldg(vb + r.vid[i]);
-    r.b[i] = __ldg(a.bary + 3 * e + i);
+    r.b[i] = sr.b[i];
   }
   // (c0 b0 + c1 b1) + c2 b2 per coordinate (interpolate.py:24-63).
   r.c.x = __fadd_rn(__fadd_rn(__fmul_rn(r.V[0].x, r.b[0]), __fmul_rn(r.V[1].x, r.b[1])),
@@ -88,9 +105,10 @@ __global__ void __launch_bounds__(256) positions_fwd_kernel(PosArgs a, Batch B) 
   const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
   float4 c = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
   float fg = 0.0f;
-  if (__ldg(a.z + r.e) != 1.0f) {
+  const SampleRef sr = load_sample(a, r.e);
+  if (sr.z != 1.0f) {
     fg = 1.0f;
-    c = interpolate_clip(a, B, r.img, r.e).c;
+    c = interpolate_clip(a, B, r.img, sr).c;
   }
   // viewport = ((xyz / w + 1) * (W, H, 1)) * 0.5
   const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
@@ -104,8 +122,8 @@ __global__ void __launch_bounds__(256) positions_bwd_kernel(PosArgs a, Batch B) 
   if (q >= int64_t(a.L) * B.pix_prefix[B.n]) return;
   const PixelRef r = decode(B, a.L, q);
   const float4 g = a.dvp[r.e];
-  const bool fg = __ldg(a.z + r.e) != 1.0f;
-  if (!fg || (g.x == 0.0f && g.y == 0.0f)) {
+  const SampleRef sr = load_sample(a, r.e);
+  if (sr.z == 1.0f || (g.x == 0.0f && g.y == 0.0f)) {
     if (a.d_bary) {
       a.d_bary[3 * r.e] = 0.0f;
       a.d_bary[3 * r.e + 1] = 0.0f;
@@ -113,7 +131,7 @@ __global__ void __launch_bounds__(256) positions_bwd_kernel(PosArgs a, Batch B) 
     }
     return;
   }
-  const Interp it = interpolate_clip(a, B, r.img, r.e);
+  const Interp it = interpolate_clip(a, B, r.img, sr);
   const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
   // viewport z carries no gradient (it only enters comparisons).
   const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
@@ -194,9 +212,10 @@ __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B)
   float4 c = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
   float fg = 0.0f;
   float* o = a.attr_out + r.e * K;
-  if (__ldg(p.z + r.e) != 1.0f) {
+  const SampleRef sr = load_sample(p, r.e);
+  if (sr.z != 1.0f) {
     fg = 1.0f;
-    const Interp it = interpolate_clip(p, B, r.img, r.e);
+    const Interp it = interpolate_clip(p, B, r.img, sr);
     c = it.c;
     const float* ab = a.attr + B.vertex_offset[r.img] * K;
     const float* a0 = ab + int64_t(it.vid[0]) * K;
@@ -226,7 +245,9 @@ __global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B)
   const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (q >= int64_t(p.L) * B.pix_prefix[B.n]) return;
   const PixelRef r = decode(B, p.L, q);
-  if (__ldg(p.z + r.e) == 1.0f) {
+  const SampleRef sr = load_sample(p, r.e);
+  const float4 g = p.dvp ? __ldg(p.dvp + r.e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (sr.z == 1.0f) {
     if (p.d_bary) {
       p.d_bary[3 * r.e] = 0.0f;
       p.d_bary[3 * r.e + 1] = 0.0f;
@@ -234,9 +255,8 @@ __global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B)
     }
     return;
   }
-  const Interp it = interpolate_clip(p, B, r.img, r.e);
+  const Interp it = interpolate_clip(p, B, r.img, sr);
   float db[3] = {0.0f, 0.0f, 0.0f};
-  const float4 g = p.dvp ? __ldg(p.dvp + r.e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (g.x != 0.0f || g.y != 0.0f) {
     // viewport z carries no gradient (it only enters comparisons).
     const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
