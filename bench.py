@@ -192,12 +192,10 @@ def kernel_bytes(wl, fg, C=4, K=4):
   L, P, T, V = wl.num_layers, wl.pixels, wl.triangles, wl.vertices
   S = L * P
   return {
-      # triangle indices and clip vertices in; ids, z, bary of every sample out
-      "raster": T * 12 + V * 16 + 20 * S,
-      # z of every sample, ids + bary of the foreground ones and the mesh
-      # (indices, clip vertices, attributes) in; K attributes and the
+      # rasterizer with the fused interpolation epilogue: the mesh (indices,
+      # clip vertices, attributes) in; ids, z, bary, K attributes and the
       # viewport position of every sample out
-      "samples_fwd": 4 * S + 16 * fg + T * 12 + V * (16 + 4 * K) + S * (4 * K + 16),
+      "raster": T * 12 + V * (16 + 4 * K) + S * (20 + 4 * K + 16),
       # position of every sample and color of every foreground sample in;
       # composited color and saved accumulators (3 (C + 1)) per pixel out
       "splat_fwd": 16 * S + 4 * C * fg + P * (4 * C + 12 * (C + 1)),

@@ -46,6 +46,8 @@ SIGNATURES = {
     "dr_abi_version": (_I, []),
     "dr_rasterize_batch_workspace_bytes": (_S, [_P, _I, _P]),
     "dr_rasterize_batch": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _S, _P]),
+    "dr_rasterize_batch_interpolate": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P,
+                                           _P, _S, _P]),
     "dr_rasterize_triangles_workspace_bytes": (_S, [_I, _I, _I, _I]),
     "dr_rasterize_triangles": (_I, [_P, _I, _P, _I, _I, _I, _I, _I, _I, _P, _P,
                                     _P, _P, _S, _P]),

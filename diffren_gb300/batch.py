@@ -7,9 +7,9 @@ needs equal shapes. ``BatchRenderer`` instead packs a fixed ragged batch
 (per-mesh triangle lists and per-image resolutions) once, keeps its own
 rasterizer workspace, and renders all images with one launch sequence:
 transform, setup + tile binning + the persistent fine rasterizer over the
-batch's (image, tile) queue, interpolation fused with the splat positions,
-the user's shader on the packed buffers, splat/normalize/composite, and the
-VJP kernels. Because no call
+batch's (image, tile) queue whose epilogue also interpolates the attributes
+and the splat positions, the user's shader on the packed buffers,
+splat/normalize/composite, and the VJP kernels. Because no call
 allocates outside torch's allocator or synchronizes, a whole forward+backward
 step can be captured in a CUDA graph (``torch.cuda.graph``) and replayed.
 
@@ -84,18 +84,24 @@ class BatchRenderer:
     else:
       clip = kernels.transform(vertices.float().contiguous(),
                                torch.as_tensor(cameras, device=self.device), b)
-    ids, z, bary = self.rasterize(clip)
     L = self.num_layers
     keys = list(attributes.keys())
     parts = [kernels._f32(attributes[k], self.device) for k in keys]
     widths = [p.shape[1] for p in parts]
     cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0]
     splatting = compositing_mode == constants.CompositingMode.SPLAT_OVER
-    if splatting:
-      interp, vp = kernels.interpolate_with_positions_packed(cat, clip, bary,
-                                                             self.triangles, ids, z, b, L)
+    if splatting and cat.shape[1] <= kernels._lib.DR_MAX_CHANNELS:
+      # One pass: the rasterizer's epilogue interpolates the attributes and
+      # the splat positions of every layer sample.
+      interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
+          cat, clip, self.triangles, b, self.config, self.workspace)
     else:
-      interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
+      ids, z, bary = self.rasterize(clip)
+      if splatting:
+        interp, vp = kernels.interpolate_with_positions_packed(cat, clip, bary,
+                                                               self.triangles, ids, z, b, L)
+      else:
+        interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
     split = torch.split(interp, widths, dim=1)
     shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
     shaded = shaded.reshape(-1, shaded.shape[-1])

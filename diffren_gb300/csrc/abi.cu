@@ -74,6 +74,22 @@ int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
                 err);
 }
 
+int dr_rasterize_batch_interpolate(const float* vertices, const int32_t* triangles,
+                                   const dr_image_desc* images, int32_t num_images,
+                                   const dr_raster_config* config, int32_t* triangle_ids,
+                                   float* z_buffer, float* barycentrics,
+                                   const float* attributes, int32_t num_channels,
+                                   float* attributes_out, float* positions, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  std::string err;
+  dr::SampleOutputs so{attributes, num_channels, attributes_out,
+                       reinterpret_cast<float4*>(positions)};
+  return finish(dr::raster_launch(vertices, triangles, images, num_images, config,
+                                  triangle_ids, z_buffer, barycentrics, workspace,
+                                  workspace_bytes, as_stream(stream), err, &so),
+                err);
+}
+
 size_t dr_rasterize_triangles_workspace_bytes(int32_t num_triangles,
                                               int32_t image_width,
                                               int32_t image_height,

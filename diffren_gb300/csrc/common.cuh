@@ -60,6 +60,60 @@ __device__ __forceinline__ PixelRef decode(const Batch& B, int L, int64_t q) {
   return r;
 }
 
+// Optional outputs of the rasterizer's epilogue: per layer sample the splat
+// position (viewport xyz + foreground flag) and the interpolated attributes.
+struct SampleOutputs {
+  const float* attr;  // [V, K] packed per mesh (nullable)
+  int K;
+  float* attr_out;    // [L * P, K]
+  float4* positions;  // [L * P]; null = no fused outputs
+};
+
+// ------------------------------------------------------- sample helpers
+// Channels k0 .. k0 + n - 1 (n <= 4) of a row; `vec` when the row is
+// 16-byte aligned and holds 4 channels from k0.
+__device__ __forceinline__ float4 load_chunk(const float* p, int n, bool vec) {
+  if (vec) return __ldg(reinterpret_cast<const float4*>(p));
+  float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  v.x = __ldg(p);
+  if (n > 1) v.y = __ldg(p + 1);
+  if (n > 2) v.z = __ldg(p + 2);
+  if (n > 3) v.w = __ldg(p + 3);
+  return v;
+}
+
+__device__ __forceinline__ void store_chunk(float* p, float4 v, int n, bool vec) {
+  if (vec) {
+    *reinterpret_cast<float4*>(p) = v;
+    return;
+  }
+  p[0] = v.x;
+  if (n > 1) p[1] = v.y;
+  if (n > 2) p[2] = v.z;
+  if (n > 3) p[3] = v.w;
+}
+
+// (a0 b0 + a1 b1) + a2 b2 per channel (interpolate.py:24-63).
+__device__ __forceinline__ float lerp3(float a0, float a1, float a2, const float b[3]) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b[0]), __fmul_rn(a1, b[1])), __fmul_rn(a2, b[2]));
+}
+
+// Splat position of a layer sample (splat.py:207-221): viewport
+// ((xyz / w + 1) * (W, H, 1)) * 0.5 of the interpolated clip coordinates c
+// ((0, 0, 1, 1) on background), with the foreground flag in w.
+__device__ __forceinline__ float4 viewport_of(float4 c, float W, float H, float fg) {
+  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
+  return make_float4(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.0f), W), 0.5f),
+                     __fmul_rn(__fmul_rn(__fadd_rn(ny, 1.0f), H), 0.5f),
+                     __fmul_rn(__fmul_rn(__fadd_rn(nz, 1.0f), 1.0f), 0.5f), fg);
+}
+
+// (c0 b0 + c1 b1) + c2 b2 per coordinate of three clip vertices.
+__device__ __forceinline__ float4 lerp_clip(float4 v0, float4 v1, float4 v2, const float b[3]) {
+  return make_float4(lerp3(v0.x, v1.x, v2.x, b), lerp3(v0.y, v1.y, v2.y, b),
+                     lerp3(v0.z, v1.z, v2.z, b), lerp3(v0.w, v1.w, v2.w, b));
+}
+
 // ------------------------------------------------------------ exact math
 // Float-to-integer conversions round toward zero, saturate and map NaN to 0
 // (cvt.rzi); int64-to-float rounds to nearest. The CPU checker implements

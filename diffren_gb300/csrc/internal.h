@@ -69,7 +69,8 @@ size_t raster_workspace_bytes(const dr_image_desc* images, int n,
 int raster_launch(const float* vertices, const int32_t* triangles,
                   const dr_image_desc* images, int n, const dr_raster_config* cfg,
                   int32_t* ids, float* z, float* bary, void* workspace,
-                  size_t ws_bytes, cudaStream_t stream, std::string& err);
+                  size_t ws_bytes, cudaStream_t stream, std::string& err,
+                  const SampleOutputs* samples = nullptr);
 int depth_codec_selftest(unsigned long long* out, cudaStream_t stream, std::string& err);
 // Byte offset of the device error word inside a raster workspace.
 constexpr size_t kErrorFlagsOffset = 4;

@@ -49,6 +49,7 @@ struct RasterArgs {
   int32_t* ids;
   float* z;
   float* bary;
+  SampleOutputs so;
 };
 
 // Workspace: the zeroed block first, then the rest; 256-byte aligned parts.
@@ -232,7 +233,51 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 // and spreads the (triangle, pixel) candidates of each chunk of the tile's
 // triangles evenly over its threads (block prefix scan + binary search), so
 // large and small triangles cost the same per pixel.
-__global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Batch B) {
+// Fused interpolation of one layer sample o with triangle `id` and the
+// barycentrics just written: the splat position (splat.py:207-221) and, when
+// requested, the attributes (interpolate.py:24-63, background 0). The same
+// operations, in the same order, as samples_fwd_kernel on the stored buffers.
+__device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B, int img, int id,
+                                          float zz, const float b[3], int64_t o) {
+  const SampleOutputs& so = a.so;
+  const int K = so.K;
+  const bool vec_rows = (K & 3) == 0;
+  float4 c = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
+  float* ao = so.attr ? so.attr_out + o * K : nullptr;
+  const bool fg = zz != 1.0f;
+  if (fg) {
+    const int32_t* t = a.tris + 3 * (B.triangle_offset[img] + id);
+    const int v0 = __ldg(t), v1 = __ldg(t + 1), v2 = __ldg(t + 2);
+    const float4* vb = a.verts + B.vertex_offset[img];
+    c = lerp_clip(__ldg(vb + v0), __ldg(vb + v1), __ldg(vb + v2), b);
+    if (ao) {
+      const float* ab = so.attr + B.vertex_offset[img] * K;
+      const float* a0 = ab + int64_t(v0) * K;
+      const float* a1 = ab + int64_t(v1) * K;
+      const float* a2 = ab + int64_t(v2) * K;
+      for (int k = 0; k < K; k += 4) {
+        const int n = min(4, K - k);
+        const float4 x = load_chunk(a0 + k, n, vec_rows), y = load_chunk(a1 + k, n, vec_rows),
+                     w = load_chunk(a2 + k, n, vec_rows);
+        store_chunk(ao + k,
+                    make_float4(lerp3(x.x, y.x, w.x, b), lerp3(x.y, y.y, w.y, b),
+                                lerp3(x.z, y.z, w.z, b), lerp3(x.w, y.w, w.w, b)),
+                    n, vec_rows);
+      }
+    }
+  } else if (ao) {
+    for (int k = 0; k < K; k += 4)
+      store_chunk(ao + k, make_float4(0.0f, 0.0f, 0.0f, 0.0f), min(4, K - k), vec_rows);
+  }
+  so.positions[o] = viewport_of(c, __int2float_rn(B.width[img]), __int2float_rn(B.height[img]),
+                                fg ? 1.0f : 0.0f);
+}
+
+// kFused adds the sample outputs to the epilogue; it needs more registers,
+// so it is a separate instantiation with its own occupancy.
+template <bool kFused>
+__global__ void __launch_bounds__(kThreads, kFused ? 4 : 5) fine_raster_kernel(RasterArgs a,
+                                                                             Batch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_warp[kThreads / 32];
   __shared__ int s_item;
@@ -378,7 +423,8 @@ __global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Bat
     }
 
     // Epilogue: unpack, recompute barycentrics (and float depth) of the
-    // winning triangle at each pixel, write all L layers.
+    // winning triangle at each pixel, write all L layers; optionally also
+    // each layer sample's splat position and interpolated attributes.
     const int64_t HW = int64_t(H) * W;
     const int64_t base = int64_t(L) * B.pix_off[img];
     for (int p = threadIdx.x; p < TP; p += kThreads) {
@@ -419,6 +465,7 @@ __global__ void __launch_bounds__(kThreads) fine_raster_kernel(RasterArgs a, Bat
         bo[0] = b[0];
         bo[1] = b[1];
         bo[2] = b[2];
+        if (kFused) write_sample(a, B, img, id, zz, b, o);
       }
     }
     __syncthreads();
@@ -453,6 +500,36 @@ __global__ void depth_codec_selftest_kernel(unsigned long long* out) {
       atomicMin(&out[1], (unsigned long long)u);
     }
   }
+}
+
+// Raises the fine rasterizer's dynamic shared-memory limit and computes its
+// persistent grid (resident blocks per SM x SMs), once per instantiation
+// and shared-memory size (host-side attributes only).
+template <bool kFused>
+bool prepare_fine(size_t smem, int& sms, int& per_sm, std::string& err) {
+  static size_t smem_set = 0, occ_smem = 0;
+  static int s_sms = 0, s_per_sm = 0;
+  if (smem > 48 * 1024 && smem > smem_set) {
+    if (cudaFuncSetAttribute(fine_raster_kernel<kFused>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem)) != cudaSuccess) {
+      err = "tile and layer count need more shared memory than the device has";
+      return false;
+    }
+    smem_set = smem;
+  }
+  if (occ_smem != smem) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per_sm, fine_raster_kernel<kFused>,
+                                                  kThreads, smem);
+    if (s_per_sm < 1) s_per_sm = 1;
+    occ_smem = smem;
+  }
+  sms = s_sms;
+  per_sm = s_per_sm;
+  return true;
 }
 
 int resolve_tile(int v) { return v > 0 ? v : kDefaultTile; }
@@ -510,7 +587,8 @@ size_t raster_workspace_bytes(const dr_image_desc* images, int n,
 int raster_launch(const float* vertices, const int32_t* triangles,
                   const dr_image_desc* images, int n, const dr_raster_config* cfg,
                   int32_t* ids, float* z, float* bary, void* workspace,
-                  size_t ws_bytes, cudaStream_t stream, std::string& err) {
+                  size_t ws_bytes, cudaStream_t stream, std::string& err,
+                  const SampleOutputs* samples) {
   int L, TW, TH, large;
   if (!check_config(cfg, L, TW, TH, large, err)) return DR_ERR_INVALID_ARGUMENT;
   if (n < 0 || (n > 0 && !images)) { err = "invalid image table"; return DR_ERR_INVALID_ARGUMENT; }
@@ -524,27 +602,30 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     err = "vertices must be 16-byte aligned and the workspace 256-byte aligned";
     return DR_ERR_MISALIGNED;
   }
-  const size_t smem = fine_smem_bytes(L, TW, TH);
-  static size_t smem_set = 0;
-  if (smem > 48 * 1024 && smem > smem_set) {
-    if (cudaFuncSetAttribute(fine_raster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem)) != cudaSuccess) {
-      err = "tile and layer count need more shared memory than the device has";
+  SampleOutputs so{};
+  if (samples) {
+    so = *samples;
+    if (!so.positions || (so.attr && (!so.attr_out || so.K < 1 || so.K > DR_MAX_CHANNELS))) {
+      err = "positions must be non-null, and attributes need attributes_out and 1 to 16 "
+            "channels";
       return DR_ERR_INVALID_ARGUMENT;
     }
-    smem_set = smem;
+    if (!so.attr) so.K = 0;
+    const bool vec = so.attr && so.K % 4 == 0;
+    if ((reinterpret_cast<uintptr_t>(so.positions) & 15) != 0 ||
+        (vec && ((reinterpret_cast<uintptr_t>(so.attr) & 15) != 0 ||
+                 (reinterpret_cast<uintptr_t>(so.attr_out) & 15) != 0))) {
+      err = "positions (and, with a multiple of 4 channels, the attribute buffers) must be "
+            "16-byte aligned";
+      return DR_ERR_MISALIGNED;
+    }
   }
-  // Persistent grid: resident blocks per SM x SMs (cached per smem size).
-  static size_t occ_smem = 0;
-  static int sms = 0, per_sm = 0;
-  if (occ_smem != smem) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fine_raster_kernel, kThreads, smem);
-    if (per_sm < 1) per_sm = 1;
-    occ_smem = smem;
-  }
+  const size_t smem = fine_smem_bytes(L, TW, TH);
+  const bool fused = so.positions != nullptr;
+  int sms = 0, per_sm = 0;
+  if (!(fused ? prepare_fine<true>(smem, sms, per_sm, err)
+              : prepare_fine<false>(smem, sms, per_sm, err)))
+    return DR_ERR_INVALID_ARGUMENT;
 
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
     const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
@@ -578,6 +659,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     a.ids = ids;
     a.z = z;
     a.bary = bary;
+    a.so = so;
 
     if (cudaMemsetAsync(ws, 0, lay.zero_end, stream) != cudaSuccess) {
       err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(cudaGetLastError());
@@ -593,7 +675,10 @@ int raster_launch(const float* vertices, const int32_t* triangles,
       bin_scatter_kernel<<<grid, 256, 0, stream>>>(a, b);
     }
     const int blocks = std::max(1, std::min(tiles, sms * per_sm));
-    fine_raster_kernel<<<blocks, kThreads, smem, stream>>>(a, b);
+    if (fused)
+      fine_raster_kernel<true><<<blocks, kThreads, smem, stream>>>(a, b);
+    else
+      fine_raster_kernel<false><<<blocks, kThreads, smem, stream>>>(a, b);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       err = std::string("raster launch failed: ") + cudaGetErrorString(e);

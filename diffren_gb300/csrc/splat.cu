@@ -110,11 +110,7 @@ __global__ void __launch_bounds__(256) positions_fwd_kernel(PosArgs a, Batch B) 
     fg = 1.0f;
     c = interpolate_clip(a, B, r.img, sr).c;
   }
-  // viewport = ((xyz / w + 1) * (W, H, 1)) * 0.5
-  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
-  a.vp[r.e] = make_float4(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.0f), W), 0.5f),
-                          __fmul_rn(__fmul_rn(__fadd_rn(ny, 1.0f), H), 0.5f),
-                          __fmul_rn(__fmul_rn(__fadd_rn(nz, 1.0f), 1.0f), 0.5f), fg);
+  a.vp[r.e] = viewport_of(c, W, H, fg);
 }
 
 __global__ void __launch_bounds__(256) positions_bwd_kernel(PosArgs a, Batch B) {
@@ -162,29 +158,6 @@ struct SampleArgs {
   float* d_attr;            // [V, K] accumulated
 };
 
-// Channels k0 .. k0 + n - 1 (n <= 4) of a row; `vec` when the row is
-// 16-byte aligned and holds 4 channels from k0.
-__device__ __forceinline__ float4 load_chunk(const float* p, int n, bool vec) {
-  if (vec) return __ldg(reinterpret_cast<const float4*>(p));
-  float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  v.x = __ldg(p);
-  if (n > 1) v.y = __ldg(p + 1);
-  if (n > 2) v.z = __ldg(p + 2);
-  if (n > 3) v.w = __ldg(p + 3);
-  return v;
-}
-
-__device__ __forceinline__ void store_chunk(float* p, float4 v, int n, bool vec) {
-  if (vec) {
-    *reinterpret_cast<float4*>(p) = v;
-    return;
-  }
-  p[0] = v.x;
-  if (n > 1) p[1] = v.y;
-  if (n > 2) p[2] = v.z;
-  if (n > 3) p[3] = v.w;
-}
-
 __device__ __forceinline__ void add_chunk(float* p, float4 v, int n, bool vec) {
   if (vec) {
     atomicAdd(reinterpret_cast<float4*>(p), v);
@@ -194,11 +167,6 @@ __device__ __forceinline__ void add_chunk(float* p, float4 v, int n, bool vec) {
   if (n > 1) atomicAdd(p + 1, v.y);
   if (n > 2) atomicAdd(p + 2, v.z);
   if (n > 3) atomicAdd(p + 3, v.w);
-}
-
-// (a0 b0 + a1 b1) + a2 b2 per channel (interpolate.py:24-63).
-__device__ __forceinline__ float lerp3(float a0, float a1, float a2, const float b[3]) {
-  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b[0]), __fmul_rn(a1, b[1])), __fmul_rn(a2, b[2]));
 }
 
 __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B) {
@@ -234,10 +202,7 @@ __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B)
     for (int k = 0; k < K; k += 4)
       store_chunk(o + k, make_float4(0.0f, 0.0f, 0.0f, 0.0f), min(4, K - k), vec_rows);
   }
-  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
-  p.vp[r.e] = make_float4(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.0f), W), 0.5f),
-                          __fmul_rn(__fmul_rn(__fadd_rn(ny, 1.0f), H), 0.5f),
-                          __fmul_rn(__fmul_rn(__fadd_rn(nz, 1.0f), 1.0f), 0.5f), fg);
+  p.vp[r.e] = viewport_of(c, W, H, fg);
 }
 
 __global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B) {

@@ -408,28 +408,84 @@ class _Samples(torch.autograd.Function):
   @staticmethod
   def backward(ctx, d_out, d_vp):
     attributes, clip, bary, triangles, ids, z = ctx.saved_tensors
-    lib = _lib.load()
-    none = (None,) * 6
-    if d_out is None and d_vp is None:
-      return (None, None, None) + none[:5]
-    if d_out is not None:
-      d_out = d_out.contiguous()
-    if d_vp is not None:
-      d_vp = d_vp.contiguous()
-      if d_vp.data_ptr() % 16:
-        d_vp = d_vp.clone()
-    d_attr = torch.zeros_like(attributes)
-    d_clip = torch.zeros_like(clip)
-    d_bary = torch.empty_like(bary) if ctx.needs_input_grad[2] else None
-    with _op("samples_bwd", _groups(ctx.batch)):
-      rc = lib.dr_interpolate_with_positions_bwd(
-          _p(d_out), _p(d_vp), _p(attributes), attributes.shape[1], _p(clip),
-          _p(triangles), _p(ids), _p(z), _p(bary), ctx.batch.ptr, ctx.batch.n, ctx.L,
-          _p(d_attr), _p(d_clip), _p(d_bary), _stream(clip.device))
-    _lib.check(rc, "dr_interpolate_with_positions_bwd")
+    d_attr, d_clip, d_bary = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary,
+                                          triangles, ids, z, ctx.needs_input_grad[2])
     return (d_attr if ctx.needs_input_grad[0] else None,
             d_clip if ctx.needs_input_grad[1] else None,
             d_bary, None, None, None, None, None)
+
+
+def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, want_bary):
+  """(d attributes, d clip, d barycentrics or None) of the fused pass."""
+  lib = _lib.load()
+  if d_out is None and d_vp is None:
+    return None, None, None
+  if d_out is not None:
+    d_out = d_out.contiguous()
+  if d_vp is not None:
+    d_vp = d_vp.contiguous()
+    if d_vp.data_ptr() % 16:
+      d_vp = d_vp.clone()
+  d_attr = torch.zeros_like(attributes)
+  d_clip = torch.zeros_like(clip)
+  d_bary = torch.empty_like(bary) if want_bary else None
+  with _op("samples_bwd", _groups(ctx.batch)):
+    rc = lib.dr_interpolate_with_positions_bwd(
+        _p(d_out), _p(d_vp), _p(attributes), attributes.shape[1], _p(clip),
+        _p(triangles), _p(ids), _p(z), _p(bary), ctx.batch.ptr, ctx.batch.n, ctx.L,
+        _p(d_attr), _p(d_clip), _p(d_bary), _stream(clip.device))
+  _lib.check(rc, "dr_interpolate_with_positions_bwd")
+  return d_attr, d_clip, d_bary
+
+
+class _RasterSamples(torch.autograd.Function):
+  """Rasterization fused with attribute interpolation and splat positions;
+  the VJP is that of the fused pass (the rasterizer's own outputs carry no
+  gradient, as in the reference)."""
+
+  @staticmethod
+  def forward(ctx, attributes, clip, triangles, batch, config, workspace):
+    lib = _lib.load()
+    dev = clip.device
+    L = config.num_layers
+    n = L * batch.total_pixels
+    K = attributes.shape[1]
+    ids = torch.empty(n, dtype=torch.int32, device=dev)
+    z = torch.empty(n, dtype=torch.float32, device=dev)
+    bary = torch.empty(n, 3, dtype=torch.float32, device=dev)
+    out = torch.empty(n, K, dtype=torch.float32, device=dev)
+    vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
+    ws = workspace.get(raster_workspace_bytes(batch, config))
+    with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
+      rc = lib.dr_rasterize_batch_interpolate(
+          _p(clip), _p(triangles), batch.ptr, batch.n, ctypes.byref(config), _p(ids), _p(z),
+          _p(bary), _p(attributes), K, _p(out), _p(vp), _p(ws), ws.numel(), _stream(dev))
+    _lib.check(rc, "dr_rasterize_batch_interpolate")
+    ctx.save_for_backward(attributes, clip, bary, triangles, ids, z)
+    ctx.batch, ctx.L = batch, L
+    ctx.set_materialize_grads(False)
+    ctx.mark_non_differentiable(ids, z, bary)
+    return out, vp, ids, z, bary
+
+  @staticmethod
+  def backward(ctx, d_out, d_vp, *unused):
+    attributes, clip, bary, triangles, ids, z = ctx.saved_tensors
+    d_attr, d_clip, _ = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles,
+                                     ids, z, False)
+    return (d_attr if ctx.needs_input_grad[0] else None,
+            d_clip if ctx.needs_input_grad[1] else None, None, None, None, None)
+
+
+def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, workspace):
+  """Rasterizes a packed batch and, in the same pass, interpolates
+  ``attributes`` [sum V, K <= 16] (background 0) and computes the splat
+  positions. Returns (attributes [L*P, K], positions [L*P, 4], ids, z, bary);
+  the first two are differentiable w.r.t. ``attributes`` and ``clip``."""
+  _require_cuda(clip, triangles)
+  attributes = _f32(attributes)
+  if attributes.shape[1] > _lib.DR_MAX_CHANNELS:
+    raise ValueError("at most %d attribute channels" % _lib.DR_MAX_CHANNELS)
+  return _RasterSamples.apply(attributes, clip, triangles, batch, config, workspace)
 
 
 def interpolate_with_positions_packed(attributes, clip, bary, triangles, ids, z, batch,

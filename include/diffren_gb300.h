@@ -118,6 +118,22 @@ int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
                        float* z_buffer, float* barycentrics, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* dr_rasterize_batch fused with dr_interpolate_with_positions_fwd: the
+ * rasterizer's epilogue, which already holds each layer sample's triangle
+ * and barycentrics, also writes the splat position (viewport xyz, fg)
+ * `positions` [L, H_i, W_i, 4] and, when `attributes` [V, K] is non-null,
+ * the interpolated attributes `attributes_out` [L, H_i, W_i, K] (background
+ * 0) (interpolate.py:24-63, splat.py:207-221). Same bits as the separate
+ * calls; saves their re-read of ids/z/barycentrics and vertex gathers. No
+ * reference counterpart: the reference runs these as separate JAX ops. */
+int dr_rasterize_batch_interpolate(const float* vertices, const int32_t* triangles,
+                                   const dr_image_desc* images, int32_t num_images,
+                                   const dr_raster_config* config, int32_t* triangle_ids,
+                                   float* z_buffer, float* barycentrics,
+                                   const float* attributes, int32_t num_channels,
+                                   float* attributes_out, float* positions, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
 size_t dr_rasterize_triangles_workspace_bytes(int32_t num_triangles,
                                               int32_t image_width,
                                               int32_t image_height,

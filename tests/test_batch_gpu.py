@@ -1,0 +1,116 @@
+"""Ragged batches through BatchRenderer (the benchmarked path): every image
+equals its own render_triangles call, the rasterizer's fused interpolation
+equals the separate kernels bit for bit, and a CUDA-graph replay of a
+forward+backward step equals the eager step."""
+import numpy as np
+import pytest
+import torch
+
+from diffren_gb300 import batch as batch_lib
+from diffren_gb300 import constants, kernels, render, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def rgba_shader(a):
+  return a["rgba"]
+
+
+def rgba(colors):
+  return torch.cat([colors, torch.ones_like(colors[:, :1])], 1)
+
+
+def ragged_scene(seed=0):
+  meshes = [workloads.icosphere_workload(5, seed=seed),
+            workloads.soup_workload(700, seed=seed + 1, mu=-2.2, sigma=0.5),
+            workloads.icosphere_workload(3, seed=seed + 2),
+            workloads.soup_workload(300, seed=seed + 3, mu=-2.0, sigma=0.5)]
+  sizes = [(48, 40), (64, 64), (33, 57), (70, 18)]
+  eyes = workloads.sphere_eyes(len(meshes), seed=seed + 5, radius=2.6)
+  cams = [workloads.camera_matrix(e, w, h) for e, (w, h) in zip(eyes, sizes)]
+  return meshes, cams, sizes
+
+
+def test_batch_renderer_matches_per_image(device):
+  meshes, cams, sizes = ragged_scene()
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=3, device=device)
+  v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device,
+                   requires_grad=True)
+  c = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device,
+                   requires_grad=True)
+  cam = torch.tensor(np.stack(cams), device=device)
+  out = r.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
+  rng = np.random.default_rng(0)
+  g = torch.tensor(rng.standard_normal(tuple(out.shape)).astype(np.float32), device=device)
+  gv, gc = torch.autograd.grad(out, (v, c), g)
+  imgs = r.images(out)
+  gimgs = r.images(g)
+  voff = np.cumsum([0] + [len(m.vertices) for m in meshes])
+  for i, (m, cm, (w, h)) in enumerate(zip(meshes, cams, sizes)):
+    vi = torch.tensor(m.vertices, device=device, requires_grad=True)
+    ci = torch.tensor(m.colors, device=device, requires_grad=True)
+    oi = render.render_triangles(vi, {"rgba": rgba(ci)}, torch.tensor(m.triangles, device=device),
+                                 torch.tensor(cm, device=device), w, h, rgba_shader,
+                                 num_layers=3)
+    torch.testing.assert_close(imgs[i], oi, rtol=0, atol=0)
+    gvi, gci = torch.autograd.grad(oi, (vi, ci), gimgs[i])
+    sl = slice(int(voff[i]), int(voff[i + 1]))
+    torch.testing.assert_close(gv[sl], gvi, rtol=1e-4, atol=1e-4 * float(gvi.abs().max()))
+    torch.testing.assert_close(gc[sl], gci, rtol=1e-4, atol=1e-4 * float(gci.abs().max()))
+
+
+@pytest.mark.parametrize("K", [4, 3, 6])
+@pytest.mark.parametrize("depth_mode", [constants.DepthSemantics.CUDA,
+                                        constants.DepthSemantics.CPU])
+def test_fused_raster_interpolation_matches_separate_kernels(K, depth_mode, device):
+  meshes, cams, sizes = ragged_scene(seed=3)
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=3, device=device, depth_semantics=depth_mode)
+  v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device)
+  clip = kernels.transform(v, torch.tensor(np.stack(cams), device=device), r.batch)
+  rng = np.random.default_rng(K)
+  attr = torch.tensor(rng.uniform(-1, 1, (len(v), K)).astype(np.float32), device=device)
+  out, vp, ids, z, bary = kernels.rasterize_interpolate_packed(attr, clip, r.triangles, r.batch,
+                                                               r.config, r.workspace)
+  ids2, z2, bary2 = kernels.rasterize_packed(clip, r.triangles, r.batch, r.config)
+  out2, vp2 = kernels.interpolate_with_positions_packed(attr, clip, bary2, r.triangles, ids2,
+                                                        z2, r.batch, 3)
+  for a, b in [(ids, ids2), (z, z2), (bary, bary2), (out, out2), (vp, vp2)]:
+    assert torch.equal(a, b)
+
+
+def test_graph_replay_matches_eager(device):
+  meshes, cams, sizes = ragged_scene(seed=7)
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=3, device=device)
+  verts = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device)
+  cols = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device)
+  cams_t = torch.tensor(np.stack(cams), device=device)
+  target = torch.rand(r.total_pixels, 4, device=device)
+  g_v = torch.empty_like(verts)
+  loss_out = torch.empty((), device=device)
+
+  def step():
+    v = verts.detach().requires_grad_(True)
+    out = r.render(v, {"rgba": rgba(cols)}, cams_t, rgba_shader)
+    loss = (out - target).square().sum()
+    (gv,) = torch.autograd.grad(loss, (v,))
+    g_v.copy_(gv)
+    loss_out.copy_(loss.detach())
+
+  s = torch.cuda.Stream(device)
+  s.wait_stream(torch.cuda.current_stream(device))
+  with torch.cuda.stream(s):
+    for _ in range(3):
+      step()
+  torch.cuda.current_stream(device).wait_stream(s)
+  torch.cuda.synchronize(device)
+  eager_loss, eager_g = loss_out.clone(), g_v.clone()
+  graph = torch.cuda.CUDAGraph()
+  with torch.cuda.graph(graph):
+    step()
+  graph.replay()
+  torch.cuda.synchronize(device)
+  torch.testing.assert_close(loss_out, eager_loss, rtol=1e-6, atol=0)
+  torch.testing.assert_close(g_v, eager_g, rtol=1e-4, atol=1e-4 * float(eager_g.abs().max()))
