@@ -218,7 +218,7 @@ def run_ours(args, rank, world, device):
   wl = Workload(args.workload, args.num_meshes)
   r = batch_lib.BatchRenderer([m.triangles for m in wl.meshes],
                               [len(m.vertices) for m in wl.meshes], wl.sizes,
-                              num_layers=wl.num_layers, device=device)
+                              num_layers=wl.num_layers, device=device, tile="auto")
   verts_h = torch.from_numpy(np.concatenate([m.vertices for m in wl.meshes])).pin_memory()
   cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
   cams_h = torch.from_numpy(np.stack(wl.cams)).pin_memory()
@@ -315,7 +315,8 @@ def run_ours(args, rank, world, device):
   plain = None
   if not args.no_plain and rank == 0:
     plain = run_plain(wl, device, args)
-  return dict(wl=wl, fg=fg, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
+  tile = [r.config.tile_width, r.config.tile_height, r.config.large_tiles]
+  return dict(wl=wl, fg=fg, tile=tile, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
               loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
               plain=plain, renderer=r)
 
@@ -479,7 +480,7 @@ def main():
                  "num_layers": wl.num_layers,
                  "foreground_samples": res["fg"], "parallelism": "replicas" if world > 1 else "1 GPU",
                  "l2": "per-step working set of several GB > 129 MB L2",
-                 "cuda_graph": True},
+                 "cuda_graph": True, "raster_tile_autotuned": res["tile"]},
       "e2e": {"value": world * wl.pixels / res["ms_e2e"] / 1e3, "unit": "Mpix/s",
               "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
       "plain": None if res["plain"] is None else {
@@ -490,6 +491,9 @@ def main():
       "kernels_ms": {k: round(v, 4) for k, v in pk.items()},
       "kernels_gbs": {k: round(nbytes[k] / (pk[k] * 1e-3) / 1e9, 1)
                       for k in pk if k in nbytes},
+      "raster_rates": None if "raster" not in pk else {
+          "mpix_per_s": wl.pixels / (pk["raster"] * 1e-3) / 1e6,
+          "mtriangles_per_s": wl.triangles / (pk["raster"] * 1e-3) / 1e6},
       "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                    "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                    "algorithmic_bytes": nbytes[dom], "traffic": None},

@@ -32,7 +32,10 @@ class BatchRenderer:
                resolutions: Sequence, num_layers: int = 1,
                face_culling_mode=constants.FaceCullingMode.BACK,
                depth_semantics=constants.DepthSemantics.CUDA, device=None,
-               tile=(0, 0)):
+               tile=(0, 0), large_tiles=0):
+    """``tile`` = (width, height) of the rasterizer's tiles, (0, 0) for the
+    default, or "auto" to let the autotuner pick the tile and the
+    large-triangle threshold on the first render (see autotune.py)."""
     if len(triangles) != len(vertex_counts) or len(triangles) != len(resolutions):
       raise ValueError("triangles, vertex_counts and resolutions differ in length")
     self.device = torch.device(device or "cuda")
@@ -45,10 +48,28 @@ class BatchRenderer:
         torch.zeros(0, 3, dtype=torch.int32, device=self.device)
     self.num_layers = int(num_layers)
     self.face_culling_mode = int(face_culling_mode)
-    self.config = kernels.raster_config(num_layers, face_culling_mode,
-                                        int(depth_semantics), tile)
+    self._autotune = isinstance(tile, str)
+    if self._autotune and tile != "auto":
+      raise ValueError("tile must be (width, height) or 'auto'")
+    self.config = kernels.raster_config(num_layers, face_culling_mode, int(depth_semantics),
+                                        (0, 0) if self._autotune else tile, large_tiles)
     self.workspace = kernels.Workspace(self.device)
     self.workspace.get(kernels.raster_workspace_bytes(self.batch, self.config))
+
+  def autotune(self, clip, attributes=None, **kw):
+    """Picks the fastest tile / large-triangle configuration for this batch
+    on these inputs (times the rasterizer; synchronizes, so call it before
+    capturing a CUDA graph). Returns (tile_width, tile_height, large_tiles)."""
+    from . import autotune as autotune_lib
+    with torch.no_grad():
+      choice = autotune_lib.tune(clip.detach(), self.triangles, self.batch, self.config,
+                                 None if attributes is None else attributes.detach(),
+                                 self.workspace, **kw)
+    self.config = kernels.raster_config(self.config.num_layers, self.config.face_culling_mode,
+                                        self.config.depth_mode, choice[:2], choice[2])
+    self.workspace.get(kernels.raster_workspace_bytes(self.batch, self.config))
+    self._autotune = False
+    return choice
 
   @property
   def num_images(self):
@@ -90,7 +111,10 @@ class BatchRenderer:
     widths = [p.shape[1] for p in parts]
     cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0]
     splatting = compositing_mode == constants.CompositingMode.SPLAT_OVER
-    if splatting and cat.shape[1] <= kernels._lib.DR_MAX_CHANNELS:
+    fused = splatting and cat.shape[1] <= kernels._lib.DR_MAX_CHANNELS
+    if self._autotune:
+      self.autotune(clip, cat if fused else None)
+    if fused:
       # One pass: the rasterizer's epilogue interpolates the attributes and
       # the splat positions of every layer sample.
       interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(

@@ -114,3 +114,49 @@ def test_graph_replay_matches_eager(device):
   torch.cuda.synchronize(device)
   torch.testing.assert_close(loss_out, eager_loss, rtol=1e-6, atol=0)
   torch.testing.assert_close(g_v, eager_g, rtol=1e-4, atol=1e-4 * float(eager_g.abs().max()))
+
+
+def test_every_tile_configuration_gives_the_same_bits(device):
+  """Tile and bin sizes only change speed: every autotuner candidate
+  rasterizes (and interpolates) the ragged batch to the same bits."""
+  from diffren_gb300 import autotune
+  meshes, cams, sizes = ragged_scene(seed=11)
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=4, device=device)
+  v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device)
+  clip = kernels.transform(v, torch.tensor(np.stack(cams), device=device), r.batch)
+  attr = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device)
+  ref = None
+  for w, h, large in autotune.CANDIDATES:
+    cfg = kernels.raster_config(4, constants.FaceCullingMode.BACK, 0, (w, h), large)
+    res = kernels.rasterize_interpolate_packed(attr, clip, r.triangles, r.batch, cfg,
+                                               kernels.Workspace(device))
+    if ref is None:
+      ref = res
+    else:
+      for a, b in zip(res, ref):
+        assert torch.equal(a, b), (w, h, large)
+
+
+def test_autotuned_renderer_matches_default(device, tmp_path, monkeypatch):
+  from diffren_gb300 import autotune
+  monkeypatch.setenv("DIFFREN_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+  autotune.clear_memory()
+  meshes, cams, sizes = ragged_scene(seed=13)
+  args = ([m.triangles for m in meshes], [len(m.vertices) for m in meshes], sizes)
+  v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device)
+  c = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device)
+  cam = torch.tensor(np.stack(cams), device=device)
+  r0 = batch_lib.BatchRenderer(*args, num_layers=3, device=device)
+  r1 = batch_lib.BatchRenderer(*args, num_layers=3, device=device, tile="auto")
+  out0 = r0.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
+  out1 = r1.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
+  assert torch.equal(out0, out1)
+  chosen = (r1.config.tile_width, r1.config.tile_height, r1.config.large_tiles)
+  assert chosen in autotune.CANDIDATES
+  # A second renderer for the same batch class reuses the cached choice.
+  autotune.clear_memory()
+  r2 = batch_lib.BatchRenderer(*args, num_layers=3, device=device, tile="auto")
+  r2.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
+  assert (r2.config.tile_width, r2.config.tile_height, r2.config.large_tiles) == chosen
+  autotune.clear_memory()
