@@ -391,23 +391,6 @@ __device__ __forceinline__ int surface_index(const float* z, int s, int p, int L
   return mint < minc ? -t : c;
 }
 
-// Surface indexes of the 9 taps reaching pixel p of the region (0 where the
-// source lies outside the image); bit j of the result marks tap j valid.
-// Tap j = (u + 1) * 3 + (v + 1) comes from the sample at p - (u, v).
-__device__ __forceinline__ unsigned tap_surfaces(const float* z, int p, int px, int py,
-                                                 int W, int H, int L, int surf[9]) {
-  unsigned ok = 0;
-#pragma unroll
-  for (int j = 0; j < 9; ++j) {
-    const int u = j / 3 - 1, v = j % 3 - 1;
-    const int sx = px - u, sy = py - v;
-    const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
-    ok |= unsigned(in) << j;
-    surf[j] = in ? surface_index(z, p - v * kRS - u, p, L) : 0;
-  }
-  return ok;
-}
-
 // normalization_scales = 1 / (max(W - 1, 0) + 1)   (splat.py:168-169);
 // __frcp_rn is the correctly rounded reciprocal, the same value as the
 // division.
@@ -428,98 +411,133 @@ __device__ __forceinline__ void accumulate(float2 (&acc)[2 * Q], float& wacc, co
   wacc = __fadd_rn(wacc, w);
 }
 
-// Forward: per layer and halo sample the depth, the separable tap weights
-// and the color go to shared memory,
+// Forward: per halo sample, every layer's depth and a mask of its
+// foreground layers, and for foreground layers the separable tap weights and
+// the color go to shared memory,
 //   z[l][i], wx[l][u][i], wy[l][v][i] (floats), col[l][q][i] (float4),
+//   fgm[i] (bit l set when layer l of sample i is foreground),
 // every array indexed by the region sample i so that a warp reads
 // consecutive words; then each pixel gathers the 9 taps of every layer with
-// the per-tap surface test, normalizes, composites and stores.
+// the per-tap surface test, normalizes, composites and stores. Background
+// samples weigh nothing, so their weights and colors are never written or
+// read, and a tile whose region holds no foreground sample writes zeros.
 template <int C>
-__global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
+__global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArgs a, Batch B) {
   constexpr int Q = Groups<C>::Q;
   extern __shared__ __align__(16) float smem[];
+  __shared__ unsigned s_layers;
   const TileRef tr = tile_of(B);
   const int L = a.L;
   float* zs = smem;
   float* wx = zs + L * kRR;
   float* wy = wx + 3 * L * kRR;
   float4* col = reinterpret_cast<float4*>(wy + 3 * L * kRR);
+  unsigned short* fgm = reinterpret_cast<unsigned short*>(col + Q * L * kRR);
   const int W = B.width[tr.img], H = B.height[tr.img];
+  if (threadIdx.x == 0) s_layers = 0u;
+  __syncthreads();
   {
     const int64_t HW = int64_t(W) * H;
     const int64_t base = int64_t(L) * B.pix_off[tr.img];
-    for (int k = threadIdx.x; k < L * kRR; k += blockDim.x) {
-      const int l = k / kRR, i = k - l * kRR;
+    unsigned any = 0;
+    for (int i = threadIdx.x; i < kRR; i += blockDim.x) {
       const int ry = i / kRS;
       const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
-      float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-      float4 c[Q];
+      const bool in = x >= 0 && y >= 0 && x < W && y < H;
+      const int64_t e0 = base + int64_t(y) * W + x;
+      unsigned m = 0;
+      for (int l = 0; l < L; ++l) {
+        float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        if (in) q = __ldg(a.vp + e0 + l * HW);
+        zs[l * kRR + i] = q.z;
+        if (q.w != 0.0f) {
+          m |= 1u << l;
+          const Taps t = taps_of(q, a.coef);
 #pragma unroll
-      for (int g = 0; g < Q; ++g) c[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (x >= 0 && y >= 0 && x < W && y < H) {
-        const int64_t e = base + l * HW + int64_t(y) * W + x;
-        q = __ldg(a.vp + e);
-        // A background sample weighs 0 everywhere: its color is not read.
-        if (q.w != 0.0f) load_groups<C>(a.colors + e * C, c);
+          for (int u = 0; u < 3; ++u) {
+            wx[(l * 3 + u) * kRR + i] = t.ex[u];
+            wy[(l * 3 + u) * kRR + i] = t.ey[u];
+          }
+          float4 c[Q];
+          load_groups<C>(a.colors + (e0 + l * HW) * C, c);
+#pragma unroll
+          for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + i] = c[g];
+        }
       }
-      const Taps t = taps_of(q, a.coef);
-      zs[k] = q.z;
-#pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        wx[(l * 3 + u) * kRR + i] = t.ex[u];
-        wy[(l * 3 + u) * kRR + i] = t.ey[u];
-      }
-#pragma unroll
-      for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + i] = c[g];
+      fgm[i] = (unsigned short)m;
+      any |= m;
     }
+    any = __reduce_or_sync(0xffffffffu, any);
+    if ((threadIdx.x & 31) == 0 && any) atomicOr(&s_layers, any);
   }
   __syncthreads();
+  const unsigned layers = s_layers;
 
   const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
   const int px = tr.x0 + tx, py = tr.y0 + ty;
   if (px >= W || py >= H) return;
   const int p = (ty + 1) * kRS + tx + 1;
-  int surf[9];
-  const unsigned ok = tap_surfaces(zs, p, px, py, W, H, L, surf);
+  const int64_t pix = B.pix_off[tr.img] + int64_t(py) * W + px;
 
-  // Class 0 = in front of the surface, 1 = at it, 2 = behind it
-  // (splat.py:149-162), accumulated layer by layer.
-  float2 acc0[2 * Q], acc1[2 * Q], acc2[2 * Q];
+  float acc[3][4 * Q];
   float wacc[3] = {0.0f, 0.0f, 0.0f};
+  if (layers == 0) {
 #pragma unroll
-  for (int h = 0; h < 2 * Q; ++h) {
-    acc0[h] = make_float2(0.0f, 0.0f);
-    acc1[h] = acc0[h];
-    acc2[h] = acc0[h];
-  }
-  for (int l = 0; l < L; ++l) {
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 4 * Q; ++c) acc[k][c] = 0.0f;
+  } else {
+    // Per tap: the foreground layers of the sample behind it (bits 0-15, 0
+    // outside the image) and, where it carries any weight, its surface
+    // index + 16 (bits 16+). Tap j = (u + 1) * 3 + (v + 1) comes from the
+    // sample at p - (u, v).
+    unsigned tap[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
-      if (!((ok >> j) & 1)) continue;
       const int u = j / 3 - 1, v = j % 3 - 1;
+      const int sx = px - u, sy = py - v;
+      const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
       const int s = p - v * kRS - u;
-      const float wxv = wx[(l * 3 + u + 1) * kRR + s];
-      if (wxv == 0.0f) continue;
-      const float w = __fmul_rn(wxv, wy[(l * 3 + v + 1) * kRR + s]);
-      float4 c[Q];
+      const unsigned m = in ? unsigned(fgm[s]) : 0u;
+      tap[j] = m ? m | (unsigned(surface_index(zs, s, p, L) + 16) << 16) : 0u;
+    }
+    // Class 0 = in front of the surface, 1 = at it, 2 = behind it
+    // (splat.py:149-162), accumulated layer by layer.
+    float2 acc0[2 * Q], acc1[2 * Q], acc2[2 * Q];
 #pragma unroll
-      for (int g = 0; g < Q; ++g) c[g] = col[(l * Q + g) * kRR + s];
-      if (surf[j] > l)
-        accumulate<Q>(acc0, wacc[0], c, w);
-      else if (surf[j] == l)
-        accumulate<Q>(acc1, wacc[1], c, w);
-      else
-        accumulate<Q>(acc2, wacc[2], c, w);
+    for (int h = 0; h < 2 * Q; ++h) {
+      acc0[h] = make_float2(0.0f, 0.0f);
+      acc1[h] = acc0[h];
+      acc2[h] = acc0[h];
+    }
+    for (int l = 0; l < L; ++l) {
+      if (!((layers >> l) & 1u)) continue;
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        if (!((tap[j] >> l) & 1u)) continue;
+        const int sj = int(tap[j] >> 16) - 16;
+        const int u = j / 3 - 1, v = j % 3 - 1;
+        const int s = p - v * kRS - u;
+        const float w = __fmul_rn(wx[(l * 3 + u + 1) * kRR + s], wy[(l * 3 + v + 1) * kRR + s]);
+        float4 c[Q];
+#pragma unroll
+        for (int g = 0; g < Q; ++g) c[g] = col[(l * Q + g) * kRR + s];
+        if (sj > l)
+          accumulate<Q>(acc0, wacc[0], c, w);
+        else if (sj == l)
+          accumulate<Q>(acc1, wacc[1], c, w);
+        else
+          accumulate<Q>(acc2, wacc[2], c, w);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2 * Q; ++h) {
+      acc[0][2 * h] = acc0[h].x; acc[0][2 * h + 1] = acc0[h].y;
+      acc[1][2 * h] = acc1[h].x; acc[1][2 * h + 1] = acc1[h].y;
+      acc[2][2 * h] = acc2[h].x; acc[2][2 * h + 1] = acc2[h].y;
     }
   }
 
-  float acc[3][4 * Q];
-#pragma unroll
-  for (int h = 0; h < 2 * Q; ++h) {
-    acc[0][2 * h] = acc0[h].x; acc[0][2 * h + 1] = acc0[h].y;
-    acc[1][2 * h] = acc1[h].x; acc[1][2 * h + 1] = acc1[h].y;
-    acc[2][2 * h] = acc2[h].x; acc[2][2 * h + 1] = acc2[h].y;
-  }
   float n[3][C];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -527,7 +545,6 @@ __global__ void __launch_bounds__(256) splat_fwd_kernel(SplatArgs a, Batch B) {
 #pragma unroll
     for (int c = 0; c < C; ++c) n[k][c] = __fmul_rn(acc[k][c], sc);
   }
-  const int64_t pix = B.pix_off[tr.img] + int64_t(py) * W + px;
   // over: out = n2; out = n1 + (1 - a1) out; out = n0 + (1 - a0) out
   const float t1 = __fsub_rn(1.0f, n[1][C - 1]), t0 = __fsub_rn(1.0f, n[0][C - 1]);
   float o[C];
@@ -616,6 +633,28 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
   float4* gs = reinterpret_cast<float4*>(zs + L * kRR);
   float* hs = reinterpret_cast<float*>(gs + 3 * Q * kRR);
   const int64_t lbase = int64_t(L) * B.pix_off[tr.img];
+  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+  const int sx = tr.x0 + tx, sy = tr.y0 + ty;
+  const bool mine = sx < W && sy < H;
+  const int64_t ebase = lbase + int64_t(sy) * W + sx;
+  // Background samples have no splat and so no gradient: a tile without a
+  // foreground sample only writes zeros.
+  bool fg_here = false;
+  if (mine)
+    for (int l = 0; l < L && !fg_here; ++l) fg_here = __ldg(&a.vp[ebase + l * HW].w) != 0.0f;
+  if (!__syncthreads_or(fg_here)) {
+    if (mine) {
+      float dc[4 * Q];
+#pragma unroll
+      for (int c = 0; c < 4 * Q; ++c) dc[c] = 0.0f;
+      for (int l = 0; l < L; ++l) {
+        const int64_t e = ebase + l * HW;
+        store_row<C>(a.d_colors + e * C, dc);
+        a.d_vp[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < kRR; i += blockDim.x) {
     const int ry = i / kRS;
     const int qx = tr.x0 - 1 + (i - ry * kRS), qy = tr.y0 - 1 + ry;
@@ -655,9 +694,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
     }
   }
   __syncthreads();
-  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
-  const int sx = tr.x0 + tx, sy = tr.y0 + ty;
-  if (sx >= W || sy >= H) return;
+  if (!mine) return;
   const int s1 = (ty + 1) * kRS + tx + 1;  // this sample's pixel in the ring grid
   // Surface index of this sample's splat at each of the 9 pixels it reaches:
   // pixel s1 + (u, v) sees this sample as its tap (u, v).
@@ -671,7 +708,6 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
     ok |= unsigned(in) << j;
     surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
   }
-  const int64_t ebase = lbase + int64_t(sy) * W + sx;
   for (int l = 0; l < L; ++l) {
     const int64_t e = ebase + l * HW;
     const float4 q = __ldg(a.vp + e);
@@ -730,7 +766,9 @@ float gaussian_coef() {
 // Shared memory per block: z, 3 + 3 weights and the padded color groups per
 // layer sample (forward); every layer's z, the padded color adjoints and the
 // weight adjoint of the 3 classes per ring pixel (backward).
-size_t fwd_smem(int L, int C) { return size_t(L) * kRR * 4 * (7 + 4 * ((C + 3) / 4)); }
+size_t fwd_smem(int L, int C) {
+  return size_t(L) * kRR * 4 * (7 + 4 * ((C + 3) / 4)) + size_t(kRR) * 2;
+}
 size_t bwd_smem(int L, int C) {
   return size_t(L + 3 * 4 * ((C + 3) / 4) + 3) * kRR * 4;
 }
