@@ -205,31 +205,22 @@ __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B)
   p.vp[r.e] = viewport_of(c, W, H, fg);
 }
 
-__global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B) {
+// VJP of one foreground layer sample e of image img.
+__device__ __forceinline__ void sample_vjp(const SampleArgs& a, const Batch& B, int img,
+                                           int64_t e) {
   const PosArgs& p = a.pos;
-  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (q >= int64_t(p.L) * B.pix_prefix[B.n]) return;
-  const PixelRef r = decode(B, p.L, q);
-  const SampleRef sr = load_sample(p, r.e);
-  const float4 g = p.dvp ? __ldg(p.dvp + r.e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (sr.z == 1.0f) {
-    if (p.d_bary) {
-      p.d_bary[3 * r.e] = 0.0f;
-      p.d_bary[3 * r.e + 1] = 0.0f;
-      p.d_bary[3 * r.e + 2] = 0.0f;
-    }
-    return;
-  }
-  const Interp it = interpolate_clip(p, B, r.img, sr);
+  const SampleRef sr = load_sample(p, e);
+  const float4 g = p.dvp ? __ldg(p.dvp + e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const Interp it = interpolate_clip(p, B, img, sr);
   float db[3] = {0.0f, 0.0f, 0.0f};
   if (g.x != 0.0f || g.y != 0.0f) {
     // viewport z carries no gradient (it only enters comparisons).
-    const float W = __int2float_rn(B.width[r.img]), H = __int2float_rn(B.height[r.img]);
+    const float W = __int2float_rn(B.width[img]), H = __int2float_rn(B.height[img]);
     const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
     const float cw = it.c.w;
     const float4 dcl = make_float4(dnx / cw, dny / cw, 0.0f,
                                    -(dnx * it.c.x + dny * it.c.y) / (cw * cw));
-    float4* dv = p.d_clip + B.vertex_offset[r.img];
+    float4* dv = p.d_clip + B.vertex_offset[img];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const float b = it.b[i];
@@ -240,8 +231,8 @@ __global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B)
   if (a.d_attr_out) {
     const int K = a.K;
     const bool vec_rows = (K & 3) == 0;
-    const float* src = a.d_attr_out + r.e * K;
-    const int64_t aoff = B.vertex_offset[r.img] * K;
+    const float* src = a.d_attr_out + e * K;
+    const int64_t aoff = B.vertex_offset[img] * K;
     for (int k = 0; k < K; k += 4) {
       const int n = min(4, K - k);
       const float4 ga = load_chunk(src + k, n, vec_rows);
@@ -260,9 +251,48 @@ __global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B)
     }
   }
   if (p.d_bary) {
-    p.d_bary[3 * r.e] = db[0];
-    p.d_bary[3 * r.e + 1] = db[1];
-    p.d_bary[3 * r.e + 2] = db[2];
+    p.d_bary[3 * e] = db[0];
+    p.d_bary[3 * e + 1] = db[1];
+    p.d_bary[3 * e + 2] = db[2];
+  }
+}
+
+// Each thread takes kVjpSamples samples, kSamplesBlock apart: their depths
+// are loaded together, and only foreground samples (z != 1) read anything
+// else, so mostly-background layers cost one coalesced depth read.
+constexpr int kVjpSamples = 4;
+constexpr int kSamplesBlock = 256;
+
+__global__ void __launch_bounds__(kSamplesBlock) samples_bwd_kernel(SampleArgs a, Batch B) {
+  const PosArgs& p = a.pos;
+  const int64_t total = int64_t(p.L) * B.pix_prefix[B.n];
+  const int64_t q0 = int64_t(blockIdx.x) * kSamplesBlock * kVjpSamples + threadIdx.x;
+  int img[kVjpSamples];
+  int64_t e[kVjpSamples];
+  float zv[kVjpSamples];
+#pragma unroll
+  for (int u = 0; u < kVjpSamples; ++u) {
+    const int64_t q = q0 + u * kSamplesBlock;
+    zv[u] = 1.0f;
+    img[u] = -1;
+    e[u] = 0;
+    if (q < total) {
+      const PixelRef r = decode(B, p.L, q);
+      img[u] = r.img;
+      e[u] = r.e;
+      zv[u] = __ldg(p.z + r.e);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kVjpSamples; ++u) {
+    if (img[u] < 0) continue;
+    if (zv[u] != 1.0f) {
+      sample_vjp(a, B, img[u], e[u]);
+    } else if (p.d_bary) {
+      p.d_bary[3 * e[u]] = 0.0f;
+      p.d_bary[3 * e[u] + 1] = 0.0f;
+      p.d_bary[3 * e[u] + 2] = 0.0f;
+    }
   }
 }
 
@@ -432,7 +462,10 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
   float* wx = zs + L * kRR;
   float* wy = wx + 3 * L * kRR;
   float4* col = reinterpret_cast<float4*>(wy + 3 * L * kRR);
-  unsigned short* fgm = reinterpret_cast<unsigned short*>(col + Q * L * kRR);
+  // 8-bit masks while L <= 8 (keeps five 256-thread blocks per SM at C = 4).
+  unsigned char* fgm8 = reinterpret_cast<unsigned char*>(col + Q * L * kRR);
+  unsigned short* fgm16 = reinterpret_cast<unsigned short*>(fgm8);
+  const bool wide = L > 8;
   const int W = B.width[tr.img], H = B.height[tr.img];
   if (threadIdx.x == 0) s_layers = 0u;
   __syncthreads();
@@ -464,7 +497,10 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
           for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + i] = c[g];
         }
       }
-      fgm[i] = (unsigned short)m;
+      if (wide)
+        fgm16[i] = (unsigned short)m;
+      else
+        fgm8[i] = (unsigned char)m;
       any |= m;
     }
     any = __reduce_or_sync(0xffffffffu, any);
@@ -498,7 +534,7 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
       const int sx = px - u, sy = py - v;
       const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
       const int s = p - v * kRS - u;
-      const unsigned m = in ? unsigned(fgm[s]) : 0u;
+      const unsigned m = in ? (wide ? unsigned(fgm16[s]) : unsigned(fgm8[s])) : 0u;
       tap[j] = m ? m | (unsigned(surface_index(zs, s, p, L) + 16) << 16) : 0u;
     }
     // Class 0 = in front of the surface, 1 = at it, 2 = behind it
@@ -554,7 +590,10 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
     o[c] = __fadd_rn(n[0][c], __fmul_rn(t0, mid));
   }
   store_row<C>(a.out + pix * C, o);
-  if (a.saved) {
+  // The backward reads a pixel's accumulators only through taps of
+  // foreground samples next to it, and every such sample lies in this
+  // tile's region: a region without foreground leaves them unwritten.
+  if (a.saved && layers != 0) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
 #pragma unroll
@@ -767,7 +806,7 @@ float gaussian_coef() {
 // layer sample (forward); every layer's z, the padded color adjoints and the
 // weight adjoint of the 3 classes per ring pixel (backward).
 size_t fwd_smem(int L, int C) {
-  return size_t(L) * kRR * 4 * (7 + 4 * ((C + 3) / 4)) + size_t(kRR) * 2;
+  return size_t(L) * kRR * 4 * (7 + 4 * ((C + 3) / 4)) + size_t(kRR) * (L > 8 ? 2 : 1);
 }
 size_t bwd_smem(int L, int C) {
   return size_t(L + 3 * 4 * ((C + 3) / 4) + 3) * kRR * 4;
@@ -914,7 +953,10 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
     Batch b;
     if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
     const int64_t total = int64_t(L) * b.pix_prefix[cnt];
-    if (total > 0) samples_bwd_kernel<<<unsigned((total + 255) / 256), 256, 0, stream>>>(a, b);
+    const int64_t per_block = int64_t(kSamplesBlock) * kVjpSamples;
+    if (total > 0)
+      samples_bwd_kernel<<<unsigned((total + per_block - 1) / per_block), kSamplesBlock, 0,
+                           stream>>>(a, b);
   }
   return launch_status("interpolate + splat positions backward", err);
 }

@@ -292,7 +292,8 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
  * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
  * saved [3, C + 1, P] receives the fg/surface/bg accumulators and weights
  * the VJP needs, one plane of P pixels per value, P = the largest
- * pixel_offset + width * height of the images (nullable); accum and normalized [3, H, W, C] are
+ * pixel_offset + width * height of the images (nullable; written only near
+ * foreground samples, where dr_splat_bwd reads it); accum and normalized [3, H, W, C] are
  * the reference's debugging buffers (nullable). With C % 4 == 0 the color
  * and output buffers must be 16-byte aligned. */
 int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,
