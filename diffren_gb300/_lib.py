@@ -18,6 +18,7 @@ DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
 DR_MAX_BATCH_INLINE = 128
+DR_MAX_IMAGE_DIM = 32768
 DR_STATIC_SCRATCH_BYTES = 64 << 20
 
 # Every symbol the header declares, with (restype, argtypes).
@@ -68,8 +69,8 @@ SIGNATURES = {
                                               _I, _I, _P, _P, _P, _P]),
     "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
-    "dr_splat_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
-    "dr_splat_bwd": (_I, [_P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),
+    "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
+    "dr_splat_bwd": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),
 }
 
 _lib = None

@@ -130,7 +130,7 @@ class BatchRenderer:
     shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
     shaded = shaded.reshape(-1, shaded.shape[-1])
     if splatting:
-      return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers)
+      return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers, z=z)
     fg = (z != 1.0).float()[:, None]
     shaded = shaded * fg
     if compositing_mode == constants.CompositingMode.NONE:

@@ -263,23 +263,24 @@ int dr_splat_positions_bwd(const float* d_positions, const float* clip_vertices,
                 err);
 }
 
-int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,
-                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
-                 float* out, float* saved, float* accum, float* normalized, void* stream) {
+int dr_splat_fwd(const float* positions, const float* z_buffer, const float* colors,
+                 int32_t num_channels, const dr_image_desc* images, int32_t num_images,
+                 int32_t num_layers, float* out, float* saved, float* accum,
+                 float* normalized, void* stream) {
   std::string err;
-  return finish(dr::splat_fwd_launch(positions, colors, num_channels, images, num_images,
-                                     num_layers, out, saved, accum, normalized,
+  return finish(dr::splat_fwd_launch(positions, z_buffer, colors, num_channels, images,
+                                     num_images, num_layers, out, saved, accum, normalized,
                                      as_stream(stream), err),
                 err);
 }
 
-int dr_splat_bwd(const float* d_out, const float* positions, const float* colors,
-                 const float* saved, int32_t num_channels, const dr_image_desc* images,
-                 int32_t num_images, int32_t num_layers, float* d_colors,
-                 float* d_positions, void* stream) {
+int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buffer,
+                 const float* colors, const float* saved, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* d_colors, float* d_positions, void* stream) {
   std::string err;
-  return finish(dr::splat_bwd_launch(d_out, positions, colors, saved, num_channels, images,
-                                     num_images, num_layers, d_colors, d_positions,
+  return finish(dr::splat_bwd_launch(d_out, positions, z_buffer, colors, saved, num_channels,
+                                     images, num_images, num_layers, d_colors, d_positions,
                                      as_stream(stream), err),
                 err);
 }

@@ -48,15 +48,32 @@ struct PixelRef {
   int x, y;
 };
 
+// Image of flat element q, found by comparing L * pix_prefix (no 64-bit
+// division), and its element index in the packed buffers.
+__device__ __forceinline__ int locate(const Batch& B, int L, int64_t q, int64_t& local) {
+  int lo = 0, hi = B.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (int64_t(L) * B.pix_prefix[mid] <= q) lo = mid; else hi = mid - 1;
+  }
+  local = q - int64_t(L) * B.pix_prefix[lo];
+  return lo;
+}
+
 __device__ __forceinline__ PixelRef decode(const Batch& B, int L, int64_t q) {
   PixelRef r;
-  r.img = find_segment(B.pix_prefix, B.n, q / L);
-  const int64_t hw = int64_t(B.width[r.img]) * B.height[r.img];
-  const int64_t local = q - int64_t(L) * B.pix_prefix[r.img];
+  int64_t local;
+  r.img = locate(B, L, q, local);
   r.e = int64_t(L) * B.pix_off[r.img] + local;
-  r.pix = local % hw;
-  r.y = int(r.pix / B.width[r.img]);
-  r.x = int(r.pix - int64_t(r.y) * B.width[r.img]);
+  // Image sides are at most DR_MAX_IMAGE_DIM, so a layer has < 2^30 pixels:
+  // strip whole layers, then 32-bit arithmetic.
+  const uint32_t W = uint32_t(B.width[r.img]);
+  const int64_t hw = int64_t(W) * B.height[r.img];
+  while (local >= hw) local -= hw;
+  const uint32_t pix = uint32_t(local);
+  r.pix = pix;
+  r.y = int(pix / W);
+  r.x = int(pix - uint32_t(r.y) * W);
   return r;
 }
 

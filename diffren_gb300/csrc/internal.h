@@ -20,8 +20,10 @@ inline bool make_batch(const dr_image_desc* images, int n, int L, int TW, int TH
   int64_t tris = 0, tiles = 0, pix = 0;
   for (int i = 0; i < n; ++i) {
     const dr_image_desc& d = images[i];
-    if (d.width <= 0 || d.height <= 0) {
-      err = "image " + std::to_string(i) + ": width and height must be > 0";
+    if (d.width <= 0 || d.height <= 0 || d.width > DR_MAX_IMAGE_DIM ||
+        d.height > DR_MAX_IMAGE_DIM) {
+      err = "image " + std::to_string(i) + ": width and height must be in [1, " +
+            std::to_string(DR_MAX_IMAGE_DIM) + "]";
       return false;
     }
     if (d.num_triangles < 0 || d.num_vertices < 0 || d.vertex_offset < 0 ||
@@ -119,13 +121,12 @@ int positions_bwd_launch(const float* d_positions, const float* clip, const int3
                          const int32_t* ids, const float* z, const float* bary,
                          const dr_image_desc* images, int n, int L, float* d_clip,
                          float* d_bary, cudaStream_t stream, std::string& err);
-int splat_fwd_launch(const float* positions, const float* colors, int C,
+int splat_fwd_launch(const float* positions, const float* z_buffer, const float* colors, int C,
                      const dr_image_desc* images, int n, int L, float* out, float* saved,
-                     float* accum, float* normalized, cudaStream_t stream,
-                     std::string& err);
-int splat_bwd_launch(const float* d_out, const float* positions, const float* colors,
-                     const float* saved, int C, const dr_image_desc* images, int n, int L,
-                     float* d_colors, float* d_positions, cudaStream_t stream,
-                     std::string& err);
+                     float* accum, float* normalized, cudaStream_t stream, std::string& err);
+int splat_bwd_launch(const float* d_out, const float* positions, const float* z_buffer,
+                     const float* colors, const float* saved, int C,
+                     const dr_image_desc* images, int n, int L, float* d_colors,
+                     float* d_positions, cudaStream_t stream, std::string& err);
 
 }  // namespace dr

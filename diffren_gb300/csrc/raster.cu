@@ -234,15 +234,16 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 // triangles evenly over its threads (block prefix scan + binary search), so
 // large and small triangles cost the same per pixel.
 // Fused interpolation of one layer sample o with triangle `id` and the
-// barycentrics just written: the splat position (splat.py:207-221) and, when
-// requested, the attributes (interpolate.py:24-63, background 0). The same
-// operations, in the same order, as samples_fwd_kernel on the stored buffers.
+// barycentrics just written: the splat position of a foreground sample
+// (splat.py:207-221) and, when requested, the attributes (interpolate.py:24-63,
+// background 0). The same operations, in the same order, as
+// samples_fwd_kernel on the stored buffers.
 __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B, int img, int id,
                                           float zz, const float b[3], int64_t o) {
   const SampleOutputs& so = a.so;
   const int K = so.K;
   const bool vec_rows = (K & 3) == 0;
-  float4 c = make_float4(0.0f, 0.0f, 1.0f, 1.0f);
+  float4 c;
   float* ao = so.attr ? so.attr_out + o * K : nullptr;
   const bool fg = zz != 1.0f;
   if (fg) {
@@ -265,12 +266,14 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
                     n, vec_rows);
       }
     }
+    so.positions[o] = viewport_of(c, __int2float_rn(B.width[img]),
+                                  __int2float_rn(B.height[img]), 1.0f);
   } else if (ao) {
+    // Background: attributes 0; the position is left unwritten (consumers
+    // take background samples from the depth buffer).
     for (int k = 0; k < K; k += 4)
       store_chunk(ao + k, make_float4(0.0f, 0.0f, 0.0f, 0.0f), min(4, K - k), vec_rows);
   }
-  so.positions[o] = viewport_of(c, __int2float_rn(B.width[img]), __int2float_rn(B.height[img]),
-                                fg ? 1.0f : 0.0f);
 }
 
 // kFused adds the sample outputs to the epilogue; it needs more registers,

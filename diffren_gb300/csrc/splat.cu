@@ -205,100 +205,134 @@ __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B)
   p.vp[r.e] = viewport_of(c, W, H, fg);
 }
 
-// VJP of one foreground layer sample e of image img.
-__device__ __forceinline__ void sample_vjp(const SampleArgs& a, const Batch& B, int img,
-                                           int64_t e) {
-  const PosArgs& p = a.pos;
-  const SampleRef sr = load_sample(p, e);
-  const float4 g = p.dvp ? __ldg(p.dvp + e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  const Interp it = interpolate_clip(p, B, img, sr);
-  float db[3] = {0.0f, 0.0f, 0.0f};
-  if (g.x != 0.0f || g.y != 0.0f) {
-    // viewport z carries no gradient (it only enters comparisons).
-    const float W = __int2float_rn(B.width[img]), H = __int2float_rn(B.height[img]);
-    const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
-    const float cw = it.c.w;
-    const float4 dcl = make_float4(dnx / cw, dny / cw, 0.0f,
-                                   -(dnx * it.c.x + dny * it.c.y) / (cw * cw));
-    float4* dv = p.d_clip + B.vertex_offset[img];
+// Sum of v over lanes lane..last of the calling lane's run (runs are
+// contiguous lanes; `last` is the run's final lane): afterwards each run's
+// first lane holds its total. Every lane of the warp must call it.
+__device__ __forceinline__ float run_sum(float v, int lane, int last) {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float b = it.b[i];
-      atomicAdd(dv + it.vid[i], make_float4(b * dcl.x, b * dcl.y, 0.0f, b * dcl.w));
-      db[i] = it.V[i].x * dcl.x + it.V[i].y * dcl.y + it.V[i].w * dcl.w;
+  for (int d = 1; d < 32; d <<= 1) {
+    const float t = __shfl_down_sync(0xffffffffu, v, d);
+    if (lane + d <= last) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ float4 run_sum4(float4 v, int lane, int last) {
+  return make_float4(run_sum(v.x, lane, last), run_sum(v.y, lane, last),
+                     run_sum(v.z, lane, last), run_sum(v.w, lane, last));
+}
+
+constexpr int kMaxRuns = 4;  // sum runs when a warp has at most this many
+
+// One layer sample per thread. Consecutive lanes hold consecutive pixels,
+// which mostly share a triangle, and every sample of a triangle adds into
+// the same three vertex rows; so the contributions are first summed over
+// each run of lanes with the same triangle, and only the run's first lane
+// issues the atomics (same-address atomics serialize in L2). Only
+// foreground samples (z != 1) read anything beyond their depth.
+__global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B) {
+  const PosArgs& p = a.pos;
+  const int lane = threadIdx.x & 31;
+  const int64_t total = int64_t(p.L) * B.pix_prefix[B.n];
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  int img = -1;
+  int64_t e = 0;
+  bool fg = false;
+  if (q < total) {
+    const PixelRef r = decode(B, p.L, q);
+    img = r.img;
+    e = r.e;
+    fg = __ldg(p.z + e) != 1.0f;
+  }
+  int id = -1;
+  float b[3] = {0.0f, 0.0f, 0.0f};
+  float2 g = make_float2(0.0f, 0.0f);
+  int vid[3] = {0, 0, 0};
+  float4 V[3];
+  float4 dcl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (fg) {
+    id = __ldg(p.ids + e);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) b[i] = __ldg(p.bary + 3 * e + i);
+    if (p.dvp) g = __ldg(reinterpret_cast<const float2*>(p.dvp + e));
+    const int32_t* t = p.tris + 3 * (B.triangle_offset[img] + id);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) vid[i] = __ldg(t + i);
+    const float4* vb = p.clip + B.vertex_offset[img];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) V[i] = __ldg(vb + vid[i]);
+    if (g.x != 0.0f || g.y != 0.0f) {
+      // (c0 b0 + c1 b1) + c2 b2 of the clip coordinates (interpolate.py:24-63);
+      // viewport z carries no gradient (it only enters comparisons).
+      const float4 c = lerp_clip(V[0], V[1], V[2], b);
+      const float W = __int2float_rn(B.width[img]), H = __int2float_rn(B.height[img]);
+      const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
+      dcl = make_float4(dnx / c.w, dny / c.w, 0.0f, -(dnx * c.x + dny * c.y) / (c.w * c.w));
     }
+  } else if (q < total && p.d_bary) {
+    p.d_bary[3 * e] = 0.0f;
+    p.d_bary[3 * e + 1] = 0.0f;
+    p.d_bary[3 * e + 2] = 0.0f;
+  }
+  const unsigned fg_lanes = __ballot_sync(0xffffffffu, fg);
+  if (!fg_lanes) return;  // the whole warp is background
+  // Runs of lanes with the same (image, triangle); background lanes form
+  // runs that add nothing. Warps with many short runs (small triangles)
+  // skip the summation: their atomics rarely collide.
+  const long long key = fg ? (((long long)img << 32) | unsigned(id)) : -1ll;
+  const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
+  const bool combine = __popc(heads & fg_lanes) <= kMaxRuns;
+  const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
+  const int last = combine ? (later ? __ffs(later) - 2 : 31) : lane;
+  const bool leader = combine ? ((heads >> lane) & 1u) != 0 : true;
+  float db[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float bi = b[i];
+    float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
+    if (combine) {
+      cv.x = run_sum(cv.x, lane, last);
+      cv.y = run_sum(cv.y, lane, last);
+      cv.w = run_sum(cv.w, lane, last);
+    }
+    if (leader && fg && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
+      atomicAdd(p.d_clip + B.vertex_offset[img] + vid[i], cv);
+    db[i] = fg ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
   }
   if (a.d_attr_out) {
     const int K = a.K;
     const bool vec_rows = (K & 3) == 0;
     const float* src = a.d_attr_out + e * K;
-    const int64_t aoff = B.vertex_offset[img] * K;
+    const int64_t aoff = fg ? B.vertex_offset[img] * K : 0;
     for (int k = 0; k < K; k += 4) {
       const int n = min(4, K - k);
-      const float4 ga = load_chunk(src + k, n, vec_rows);
-      if (ga.x == 0.0f && ga.y == 0.0f && ga.z == 0.0f && ga.w == 0.0f) continue;
+      const float4 ga = fg ? load_chunk(src + k, n, vec_rows) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const int64_t row = aoff + int64_t(it.vid[i]) * K + k;
-        const float b = it.b[i];
-        add_chunk(a.d_attr + row, make_float4(b * ga.x, b * ga.y, b * ga.z, b * ga.w), n,
-                  vec_rows);
-        if (p.d_bary) {
-          const float4 av = load_chunk(a.attr + row, n, vec_rows);
-          db[i] += av.x * ga.x + av.y * ga.y + av.z * ga.z + av.w * ga.w;
+        const float bi = b[i];
+        float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
+        if (combine) av = run_sum4(av, lane, last);
+        const int64_t row = aoff + int64_t(vid[i]) * K + k;
+        if (leader && fg) add_chunk(a.d_attr + row, av, n, vec_rows);
+        if (fg && p.d_bary) {
+          const float4 at = load_chunk(a.attr + row, n, vec_rows);
+          db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
         }
       }
     }
   }
-  if (p.d_bary) {
+  if (fg && p.d_bary) {
     p.d_bary[3 * e] = db[0];
     p.d_bary[3 * e + 1] = db[1];
     p.d_bary[3 * e + 2] = db[2];
   }
 }
 
-// Each thread takes kVjpSamples samples, kSamplesBlock apart: their depths
-// are loaded together, and only foreground samples (z != 1) read anything
-// else, so mostly-background layers cost one coalesced depth read.
-constexpr int kVjpSamples = 4;
-constexpr int kSamplesBlock = 256;
-
-__global__ void __launch_bounds__(kSamplesBlock) samples_bwd_kernel(SampleArgs a, Batch B) {
-  const PosArgs& p = a.pos;
-  const int64_t total = int64_t(p.L) * B.pix_prefix[B.n];
-  const int64_t q0 = int64_t(blockIdx.x) * kSamplesBlock * kVjpSamples + threadIdx.x;
-  int img[kVjpSamples];
-  int64_t e[kVjpSamples];
-  float zv[kVjpSamples];
-#pragma unroll
-  for (int u = 0; u < kVjpSamples; ++u) {
-    const int64_t q = q0 + u * kSamplesBlock;
-    zv[u] = 1.0f;
-    img[u] = -1;
-    e[u] = 0;
-    if (q < total) {
-      const PixelRef r = decode(B, p.L, q);
-      img[u] = r.img;
-      e[u] = r.e;
-      zv[u] = __ldg(p.z + r.e);
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < kVjpSamples; ++u) {
-    if (img[u] < 0) continue;
-    if (zv[u] != 1.0f) {
-      sample_vjp(a, B, img[u], e[u]);
-    } else if (p.d_bary) {
-      p.d_bary[3 * e[u]] = 0.0f;
-      p.d_bary[3 * e[u] + 1] = 0.0f;
-      p.d_bary[3 * e[u] + 2] = 0.0f;
-    }
-  }
-}
-
 // -------------------------------------------------------------------- splat
 struct SplatArgs {
   const float4* vp;  // [L*P] viewport xyz + foreground flag
+  const float* zb;   // [L*P] rasterizer depth (nullable): 1 = background
   const float* colors;
   int L;
   int64_t P;     // pixels covered by the call: plane stride of `saved`
@@ -478,10 +512,14 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
       const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
       const bool in = x >= 0 && y >= 0 && x < W && y < H;
       const int64_t e0 = base + int64_t(y) * W + x;
+      // With a depth buffer, its L independent 4-byte loads find the
+      // foreground layers first; only their positions are read.
       unsigned m = 0;
+      if (in && a.zb)
+        for (int l = 0; l < L; ++l) m |= unsigned(__ldg(a.zb + e0 + l * HW) != 1.0f) << l;
       for (int l = 0; l < L; ++l) {
         float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-        if (in) q = __ldg(a.vp + e0 + l * HW);
+        if (in && (!a.zb || ((m >> l) & 1u))) q = __ldg(a.vp + e0 + l * HW);
         zs[l * kRR + i] = q.z;
         if (q.w != 0.0f) {
           m |= 1u << l;
@@ -678,10 +716,16 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
   const int64_t ebase = lbase + int64_t(sy) * W + sx;
   // Background samples have no splat and so no gradient: a tile without a
   // foreground sample only writes zeros.
-  bool fg_here = false;
-  if (mine)
-    for (int l = 0; l < L && !fg_here; ++l) fg_here = __ldg(&a.vp[ebase + l * HW].w) != 0.0f;
-  if (!__syncthreads_or(fg_here)) {
+  // Foreground layers of this thread's own sample (bit l).
+  unsigned own = 0;
+  if (mine) {
+    if (a.zb) {
+      for (int l = 0; l < L; ++l) own |= unsigned(__ldg(a.zb + ebase + l * HW) != 1.0f) << l;
+    } else {
+      for (int l = 0; l < L; ++l) own |= unsigned(__ldg(&a.vp[ebase + l * HW].w) != 0.0f) << l;
+    }
+  }
+  if (!__syncthreads_or(own != 0)) {
     if (mine) {
       float dc[4 * Q];
 #pragma unroll
@@ -689,7 +733,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
       for (int l = 0; l < L; ++l) {
         const int64_t e = ebase + l * HW;
         store_row<C>(a.d_colors + e * C, dc);
-        a.d_vp[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!a.zb) a.d_vp[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
     }
     return;
@@ -710,8 +754,15 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
       float d[C];
       load_row<C>(a.d_out + pix * C, d);
       accum_adjoint<C>(acc, wacc, d, g, h);
-      for (int l = 0; l < L; ++l)
-        zs[l * kRR + i] = __ldg(&a.vp[lbase + l * HW + int64_t(qy) * W + qx].z);
+      const int64_t eq = lbase + int64_t(qy) * W + qx;
+      if (a.zb) {
+        unsigned m = 0;
+        for (int l = 0; l < L; ++l) m |= unsigned(__ldg(a.zb + eq + l * HW) != 1.0f) << l;
+        for (int l = 0; l < L; ++l)
+          zs[l * kRR + i] = ((m >> l) & 1u) ? __ldg(&a.vp[eq + l * HW].z) : 1.0f;
+      } else {
+        for (int l = 0; l < L; ++l) zs[l * kRR + i] = __ldg(&a.vp[eq + l * HW].z);
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -749,7 +800,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
   }
   for (int l = 0; l < L; ++l) {
     const int64_t e = ebase + l * HW;
-    const float4 q = __ldg(a.vp + e);
+    const float4 q = ((own >> l) & 1u) ? __ldg(a.vp + e) : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
     float2 dcol[2 * Q];
 #pragma unroll
     for (int hh = 0; hh < 2 * Q; ++hh) dcol[hh] = make_float2(0.0f, 0.0f);
@@ -789,7 +840,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
       dc[2 * hh + 1] = dcol[hh].y;
     }
     store_row<C>(a.d_colors + e * C, dc);
-    a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
+    if (q.w != 0.0f || !a.zb) a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
   }
 }
 
@@ -953,10 +1004,7 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
     Batch b;
     if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
     const int64_t total = int64_t(L) * b.pix_prefix[cnt];
-    const int64_t per_block = int64_t(kSamplesBlock) * kVjpSamples;
-    if (total > 0)
-      samples_bwd_kernel<<<unsigned((total + per_block - 1) / per_block), kSamplesBlock, 0,
-                           stream>>>(a, b);
+    if (total > 0) samples_bwd_kernel<<<unsigned((total + 255) / 256), 256, 0, stream>>>(a, b);
   }
   return launch_status("interpolate + splat positions backward", err);
 }
@@ -998,7 +1046,7 @@ int positions_bwd_launch(const float* d_positions, const float* clip, const int3
                        "splat positions backward");
 }
 
-int splat_fwd_launch(const float* positions, const float* colors, int C,
+int splat_fwd_launch(const float* positions, const float* z_buffer, const float* colors, int C,
                      const dr_image_desc* images, int n, int L, float* out, float* saved,
                      float* accum, float* normalized, cudaStream_t stream,
                      std::string& err) {
@@ -1012,6 +1060,7 @@ int splat_fwd_launch(const float* positions, const float* colors, int C,
   }
   SplatArgs a{};
   a.vp = reinterpret_cast<const float4*>(positions);
+  a.zb = z_buffer;
   a.colors = colors;
   a.L = L;
   a.P = call_pixels(images, n);
@@ -1020,8 +1069,9 @@ int splat_fwd_launch(const float* positions, const float* colors, int C,
   return dispatch(false, C, a, images, n, stream, err);
 }
 
-int splat_bwd_launch(const float* d_out, const float* positions, const float* colors,
-                     const float* saved, int C, const dr_image_desc* images, int n, int L,
+int splat_bwd_launch(const float* d_out, const float* positions, const float* z_buffer,
+                     const float* colors, const float* saved, int C,
+                     const dr_image_desc* images, int n, int L,
                      float* d_colors, float* d_positions, cudaStream_t stream,
                      std::string& err) {
   int rc;
@@ -1038,6 +1088,7 @@ int splat_bwd_launch(const float* d_out, const float* positions, const float* co
   }
   SplatArgs a{};
   a.vp = reinterpret_cast<const float4*>(positions);
+  a.zb = z_buffer;
   a.colors = colors;
   a.L = L;
   a.P = call_pixels(images, n);

@@ -543,7 +543,7 @@ def splat_positions_packed(clip, bary, triangles, ids, z, batch, num_layers):
 class _Splat(torch.autograd.Function):
 
   @staticmethod
-  def forward(ctx, positions, colors, batch, L, want_accum):
+  def forward(ctx, positions, colors, z, batch, L, want_accum):
     lib = _lib.load()
     C = colors.shape[1]
     dev = colors.device
@@ -557,10 +557,10 @@ class _Splat(torch.autograd.Function):
       accum = torch.empty(3 * P, C, dtype=torch.float32, device=dev)
       norm = torch.empty_like(accum)
     with _op("splat_fwd", _groups(batch)):
-      rc = lib.dr_splat_fwd(_p(positions), _p(colors), C, batch.ptr, batch.n, L, _p(out),
-                            _p(saved), _p(accum), _p(norm), _stream(dev))
+      rc = lib.dr_splat_fwd(_p(positions), _p(z), _p(colors), C, batch.ptr, batch.n, L,
+                            _p(out), _p(saved), _p(accum), _p(norm), _stream(dev))
     _lib.check(rc, "dr_splat_fwd")
-    ctx.save_for_backward(positions, colors, saved)
+    ctx.save_for_backward(positions, colors, saved, z)
     ctx.batch, ctx.L = batch, L
     if want_accum:
       ctx.mark_non_differentiable(accum, norm)
@@ -569,7 +569,7 @@ class _Splat(torch.autograd.Function):
 
   @staticmethod
   def backward(ctx, d_out, *unused):
-    positions, colors, saved = ctx.saved_tensors
+    positions, colors, saved, z = ctx.saved_tensors
     lib = _lib.load()
     d_out = d_out.contiguous()
     if d_out.data_ptr() % 16:
@@ -577,18 +577,20 @@ class _Splat(torch.autograd.Function):
     d_colors = torch.empty_like(colors)
     d_pos = torch.empty_like(positions)
     with _op("splat_bwd", _groups(ctx.batch)):
-      rc = lib.dr_splat_bwd(_p(d_out), _p(positions), _p(colors), _p(saved),
+      rc = lib.dr_splat_bwd(_p(d_out), _p(positions), _p(z), _p(colors), _p(saved),
                             colors.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L,
                             _p(d_colors), _p(d_pos), _stream(d_out.device))
     _lib.check(rc, "dr_splat_bwd")
     return (d_pos if ctx.needs_input_grad[0] else None,
-            d_colors if ctx.needs_input_grad[1] else None, None, None, None)
+            d_colors if ctx.needs_input_grad[1] else None, None, None, None, None)
 
 
-def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False):
+def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False, z=None):
   """Splatted, normalized, composited images [P, C] of a packed batch.
 
-  positions [L*P, 4] (viewport xyz, fg) and colors [L*P, C]. With
+  positions [L*P, 4] (viewport xyz, fg) and colors [L*P, C]. ``z`` [L*P],
+  the rasterizer's depth, marks background samples (z == 1), whose
+  positions are then not read (nor their position gradients written). With
   ``return_accum_buffers`` also returns the accumulated and normalized
   fg/surface/bg layers, packed [3, H_i, W_i, C] per image (not
   differentiable).
@@ -602,4 +604,6 @@ def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=Fals
     raise ValueError("splatting supports at most %d channels" %
                      _lib.DR_MAX_SPLAT_CHANNELS)
   positions = positions.contiguous()
-  return _Splat.apply(positions, colors, batch, num_layers, bool(return_accum_buffers))
+  if z is not None:
+    z = z.detach().contiguous()
+  return _Splat.apply(positions, colors, z, batch, num_layers, bool(return_accum_buffers))

@@ -55,7 +55,7 @@ def splat_clip(clip, frame: fb.Framebuffer, shaded_pixels, return_accum_buffers=
   batch, tris, ids, z, bary = frame.kernel_inputs()
   colors = _shaded_flat(shaded_pixels)
   vp = kernels.splat_positions_packed(clip, bary, tris, ids, z, batch, frame.num_layers)
-  res = kernels.splat_packed(vp, colors, batch, frame.num_layers, return_accum_buffers)
+  res = kernels.splat_packed(vp, colors, batch, frame.num_layers, return_accum_buffers, z=z)
   lead = (frame.batch_size,) if frame.is_batched else ()
   return _shape_outputs(res, lead, frame.height, frame.width, colors.shape[1],
                         return_accum_buffers)

@@ -98,6 +98,7 @@ typedef struct dr_raster_config {
 #define DR_MAX_LAYERS 16
 #define DR_MAX_CHANNELS 16
 #define DR_MAX_BATCH_INLINE 128 /* larger batches are split into launches */
+#define DR_MAX_IMAGE_DIM 32768  /* largest image width or height */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* dr_last_error(void);
@@ -121,7 +122,9 @@ int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
 /* dr_rasterize_batch fused with dr_interpolate_with_positions_fwd: the
  * rasterizer's epilogue, which already holds each layer sample's triangle
  * and barycentrics, also writes the splat position (viewport xyz, fg)
- * `positions` [L, H_i, W_i, 4] and, when `attributes` [V, K] is non-null,
+ * `positions` [L, H_i, W_i, 4] of every foreground sample (background
+ * entries are left unwritten: pass z_buffer to the splat) and, when
+ * `attributes` [V, K] is non-null,
  * the interpolated attributes `attributes_out` [L, H_i, W_i, K] (background
  * 0) (interpolate.py:24-63, splat.py:207-221). Same bits as the separate
  * calls; saves their re-read of ids/z/barycentrics and vertex gathers. No
@@ -288,7 +291,11 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
 /* splat_at_pixel_centers + composite.over (splat.py:26-175,
  * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the
  * per-tap surface test, normalization and back-to-front over compositing.
- * positions [L, H, W, 4] (viewport xyz, fg); colors [L, H, W, C]
+ * positions [L, H, W, 4] (viewport xyz, fg); z_buffer [L, H, W] (nullable)
+ * is the rasterizer's depth: samples where it is 1 are background (viewport
+ * z 1, no splat) and their positions are not read, so producers may leave
+ * them unwritten; without it every position is read and its w is the
+ * foreground flag. colors [L, H, W, C]
  * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
  * saved [3, C + 1, P] receives the fg/surface/bg accumulators and weights
  * the VJP needs, one plane of P pixels per value, P = the largest
@@ -296,17 +303,19 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
  * foreground samples, where dr_splat_bwd reads it); accum and normalized [3, H, W, C] are
  * the reference's debugging buffers (nullable). With C % 4 == 0 the color
  * and output buffers must be 16-byte aligned. */
-int dr_splat_fwd(const float* positions, const float* colors, int32_t num_channels,
-                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
-                 float* out, float* saved, float* accum, float* normalized, void* stream);
+int dr_splat_fwd(const float* positions, const float* z_buffer, const float* colors,
+                 int32_t num_channels, const dr_image_desc* images, int32_t num_images,
+                 int32_t num_layers, float* out, float* saved, float* accum,
+                 float* normalized, void* stream);
 
 /* VJP in gather form: each sample reads the adjoints of the 9 pixels it
  * reached (no atomics). Writes d_colors [L, H, W, C] and d_positions
- * [L, H, W, 4] as (d x, d y, 0, 0). `saved` is the forward's. */
-int dr_splat_bwd(const float* d_out, const float* positions, const float* colors,
-                 const float* saved, int32_t num_channels, const dr_image_desc* images,
-                 int32_t num_images, int32_t num_layers, float* d_colors,
-                 float* d_positions, void* stream);
+ * [L, H, W, 4] as (d x, d y, 0, 0); with a z_buffer, d_positions of
+ * background samples are left unwritten. `saved` is the forward's. */
+int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buffer,
+                 const float* colors, const float* saved, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* d_colors, float* d_positions, void* stream);
 
 #ifdef __cplusplus
 }

@@ -87,29 +87,43 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
                               None, None, 0, None)
   assert rc == 1
   # Too many splat channels, bad layer counts.
-  assert lib.dr_splat_fwd(None, None, 9, b.ptr, 1, 3, None, None, None, None, None) == 1
-  assert lib.dr_splat_fwd(None, None, 4, b.ptr, 1, 0, None, None, None, None, None) == 1
+  assert lib.dr_splat_fwd(None, None, None, 9, b.ptr, 1, 3, None, None, None, None,
+                          None) == 1
+  assert lib.dr_splat_fwd(None, None, None, 4, b.ptr, 1, 0, None, None, None, None,
+                          None) == 1
   # The backward needs the forward's saved accumulators.
-  assert lib.dr_splat_bwd(None, None, None, None, 4, b.ptr, 1, 3, None, None, None) == 1
+  assert lib.dr_splat_bwd(None, None, None, None, None, 4, b.ptr, 1, 3, None, None,
+                          None) == 1
   assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
                                 None) == 1
   assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1
   # Misaligned positions / clip vertices.
-  assert lib.dr_splat_fwd(ctypes.c_void_p(4), None, 4, b.ptr, 1, 3, None, None, None,
-                          None, None) == 4
+  assert lib.dr_splat_fwd(ctypes.c_void_p(4), None, None, 4, b.ptr, 1, 3, None, None,
+                          None, None, None) == 4
   assert lib.dr_splat_positions_fwd(ctypes.c_void_p(4), None, None, None, None, b.ptr, 1,
                                     3, None, None) == 4
 
 
 def test_python_constants_match_header():
   src = open(HEADER).read()
-  for name in ("DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_OK",
+  for name in ("DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_MAX_IMAGE_DIM",
+               "DR_MAX_SPLAT_CHANNELS", "DR_OK",
                "DR_CULL_NONE", "DR_CULL_BACK", "DR_CULL_FRONT", "DR_DEPTH_DISCRETIZED",
                "DR_DEPTH_FLOAT"):
     m = re.search(r"#define %s (\d+)" % name, src)
     assert m and int(m.group(1)) == getattr(_lib, name), name
   assert kernels._groups(kernels.ImageBatch([1] * 129, [1] * 129, [0] * 129,
                                             [0] * 129)) == 2
+
+
+def test_oversized_image_is_rejected():
+  lib = _lib.load()
+  cfg = kernels.raster_config(1, 0, 0)
+  ok = kernels.ImageBatch.single(_lib.DR_MAX_IMAGE_DIM, 1, 3, 1)
+  assert lib.dr_rasterize_batch_workspace_bytes(ok.ptr, 1, ctypes.byref(cfg)) > 0
+  big = kernels.ImageBatch.single(_lib.DR_MAX_IMAGE_DIM + 1, 1, 3, 1)
+  assert lib.dr_rasterize_batch_workspace_bytes(big.ptr, 1, ctypes.byref(cfg)) == 0
+  assert b"32768" in lib.dr_last_error()
 
 
 def test_status_raises_with_message():

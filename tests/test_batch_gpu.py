@@ -76,8 +76,12 @@ def test_fused_raster_interpolation_matches_separate_kernels(K, depth_mode, devi
   ids2, z2, bary2 = kernels.rasterize_packed(clip, r.triangles, r.batch, r.config)
   out2, vp2 = kernels.interpolate_with_positions_packed(attr, clip, bary2, r.triangles, ids2,
                                                         z2, r.batch, 3)
-  for a, b in [(ids, ids2), (z, z2), (bary, bary2), (out, out2), (vp, vp2)]:
+  for a, b in [(ids, ids2), (z, z2), (bary, bary2), (out, out2)]:
     assert torch.equal(a, b)
+  # The fused pass writes positions of foreground samples only.
+  fg = z != 1.0
+  assert torch.equal(vp[fg], vp2[fg])
+  assert (vp2[~fg][:, 3] == 0).all()
 
 
 def test_graph_replay_matches_eager(device):
@@ -131,6 +135,9 @@ def test_every_tile_configuration_gives_the_same_bits(device):
     cfg = kernels.raster_config(4, constants.FaceCullingMode.BACK, 0, (w, h), large)
     res = kernels.rasterize_interpolate_packed(attr, clip, r.triangles, r.batch, cfg,
                                                kernels.Workspace(device))
+    out, vp, ids, z, bary = res
+    fg = z != 1.0
+    res = (out, vp[fg], ids, z, bary)  # positions are written for foreground only
     if ref is None:
       ref = res
     else:

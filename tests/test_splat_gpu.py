@@ -99,8 +99,10 @@ def test_interpolate_backward_matches_autograd(case, device):
 
 
 def run_splat(device, clip, tris, ids, z, b, shaded, w, h, layers, accum=False,
-              requires_grad=False):
-  """Positions + splat through the C ABI; returns (clip, colors, result)."""
+              requires_grad=False, with_depth=True):
+  """Positions + splat through the C ABI; returns (clip, colors, result).
+  ``with_depth`` passes the depth buffer, so background positions are not
+  read (the rendering path); otherwise every position is read."""
   c, t, i, zz, bb, s = to_dev(device, clip, tris, ids.reshape(-1), z.reshape(-1),
                               b.reshape(-1, 3), shaded.reshape(-1, shaded.shape[-1]))
   if requires_grad:
@@ -108,7 +110,7 @@ def run_splat(device, clip, tris, ids, z, b, shaded, w, h, layers, accum=False,
     s.requires_grad_(True)
   batch = kernels.ImageBatch.single(w, h, len(clip), len(tris))
   vp = kernels.splat_positions_packed(c, bb, t, i, zz, batch, layers)
-  res = kernels.splat_packed(vp, s, batch, layers, accum)
+  res = kernels.splat_packed(vp, s, batch, layers, accum, z=zz if with_depth else None)
   return c, s, res
 
 
@@ -144,6 +146,25 @@ def test_splat_backward_matches_autograd(case, device):
   dc, ds = torch.autograd.grad(o, (c, s), torch.as_tensor(g, device=device).view(o.shape))
   assert_grad_close(ds.view(layers, h, w, C).cpu().numpy(), gs.numpy())
   assert_grad_close(dc.cpu().numpy(), gc.numpy())
+
+
+@pytest.mark.parametrize("case", [0, 2, 6])
+def test_splat_with_and_without_depth_buffer_agree(case, device):
+  """Taking background samples from the depth buffer (positions unread)
+  gives the same images and gradients as reading every position."""
+  kind, w, h, layers, C = CASES[case]
+  clip, tris, ids, z, b, shaded, _ = scene(kind, w, h, layers, C, case)
+  outs = []
+  for with_depth in (True, False):
+    c, s, out = run_splat(device, clip, tris, ids, z, b, shaded, w, h, layers,
+                          requires_grad=True, with_depth=with_depth)
+    g = torch.linspace(-1, 1, out.numel(), device=device).view(out.shape)
+    outs.append((out.detach(),) + torch.autograd.grad(out, (c, s), g))
+  (o1, dc1, ds1), (o2, dc2, ds2) = outs
+  assert torch.equal(o1, o2)
+  assert torch.equal(ds1, ds2)
+  # d clip sums float atomics, whose order varies between runs.
+  assert_grad_close(dc1.cpu().numpy(), dc2.cpu().numpy())
 
 
 def test_splat_positions_match_oracle(device):
