@@ -82,7 +82,9 @@ class DiffrenError(RuntimeError):
 
 
 def library_path():
-  return _build.LIB
+  """The in-tree build, or DIFFREN_GB300_LIBRARY when set (a prebuilt
+  library elsewhere; it is then never rebuilt)."""
+  return os.environ.get("DIFFREN_GB300_LIBRARY") or _build.LIB
 
 
 def load():
@@ -92,8 +94,8 @@ def load():
     return _lib
   with _lock:
     if _lib is None:
-      path = _build.LIB
-      if not os.path.exists(path):
+      path = library_path()
+      if path == _build.LIB and not os.path.exists(path):
         try:
           _build.build()
         except Exception as e:  # no nvcc, compile error
