@@ -223,109 +223,154 @@ __device__ __forceinline__ float4 run_sum4(float4 v, int lane, int last) {
 }
 
 constexpr int kMaxRuns = 4;  // sum runs when a warp has at most this many
+constexpr int kVjpThreads = 256;
+constexpr int kVjpPerThread = 4;  // samples whose depth each thread tests
+constexpr int kVjpBlock = kVjpThreads * kVjpPerThread;
 
-// One layer sample per thread. Consecutive lanes hold consecutive pixels,
-// which mostly share a triangle, and every sample of a triangle adds into
-// the same three vertex rows; so the contributions are first summed over
-// each run of lanes with the same triangle, and only the run's first lane
-// issues the atomics (same-address atomics serialize in L2). Only
-// foreground samples (z != 1) read anything beyond their depth.
-__global__ void __launch_bounds__(256) samples_bwd_kernel(SampleArgs a, Batch B) {
+// VJP of the interpolation and the splat positions. A block takes kVjpBlock
+// consecutive layer samples: each thread tests the depth of kVjpPerThread of
+// them, the foreground ones (z != 1) are compacted in shared memory in
+// sample order, and the block's threads then work on those densely (for
+// mostly-background images most samples cost one depth read). Consecutive
+// lanes then hold consecutive foreground samples, which mostly share a
+// triangle, and every sample of a triangle adds into the same three vertex
+// rows: contributions are summed over each run of lanes with the same
+// triangle and only the run's first lane issues the atomics (same-address
+// atomics serialize in L2).
+__global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, Batch B) {
+  __shared__ int64_t s_e[kVjpBlock];
+  __shared__ unsigned char s_img[kVjpBlock];
+  __shared__ int s_warp[kVjpThreads / 32];
   const PosArgs& p = a.pos;
   const int lane = threadIdx.x & 31;
   const int64_t total = int64_t(p.L) * B.pix_prefix[B.n];
-  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  int img = -1;
-  int64_t e = 0;
-  bool fg = false;
-  if (q < total) {
-    const PixelRef r = decode(B, p.L, q);
-    img = r.img;
-    e = r.e;
-    fg = __ldg(p.z + e) != 1.0f;
-  }
-  int id = -1;
-  float b[3] = {0.0f, 0.0f, 0.0f};
-  float2 g = make_float2(0.0f, 0.0f);
-  int vid[3] = {0, 0, 0};
-  float4 V[3];
-  float4 dcl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (fg) {
-    id = __ldg(p.ids + e);
+  const int64_t q0 = int64_t(blockIdx.x) * kVjpBlock + int64_t(threadIdx.x) * kVjpPerThread;
+  int img[kVjpPerThread];
+  int64_t e[kVjpPerThread];
+  bool fg[kVjpPerThread];
+  int nfg = 0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) b[i] = __ldg(p.bary + 3 * e + i);
-    if (p.dvp) g = __ldg(reinterpret_cast<const float2*>(p.dvp + e));
-    const int32_t* t = p.tris + 3 * (B.triangle_offset[img] + id);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) vid[i] = __ldg(t + i);
-    const float4* vb = p.clip + B.vertex_offset[img];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) V[i] = __ldg(vb + vid[i]);
-    if (g.x != 0.0f || g.y != 0.0f) {
-      // (c0 b0 + c1 b1) + c2 b2 of the clip coordinates (interpolate.py:24-63);
-      // viewport z carries no gradient (it only enters comparisons).
-      const float4 c = lerp_clip(V[0], V[1], V[2], b);
-      const float W = __int2float_rn(B.width[img]), H = __int2float_rn(B.height[img]);
-      const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
-      dcl = make_float4(dnx / c.w, dny / c.w, 0.0f, -(dnx * c.x + dny * c.y) / (c.w * c.w));
+  for (int u = 0; u < kVjpPerThread; ++u) {
+    const int64_t q = q0 + u;
+    img[u] = 0;
+    e[u] = 0;
+    fg[u] = false;
+    if (q < total) {
+      int64_t local;
+      img[u] = locate(B, p.L, q, local);
+      e[u] = int64_t(p.L) * B.pix_off[img[u]] + local;
     }
-  } else if (q < total && p.d_bary) {
-    p.d_bary[3 * e] = 0.0f;
-    p.d_bary[3 * e + 1] = 0.0f;
-    p.d_bary[3 * e + 2] = 0.0f;
   }
-  const unsigned fg_lanes = __ballot_sync(0xffffffffu, fg);
-  if (!fg_lanes) return;  // the whole warp is background
-  // Runs of lanes with the same (image, triangle); background lanes form
-  // runs that add nothing. Warps with many short runs (small triangles)
-  // skip the summation: their atomics rarely collide.
-  const long long key = fg ? (((long long)img << 32) | unsigned(id)) : -1ll;
-  const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
-  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
-  const bool combine = __popc(heads & fg_lanes) <= kMaxRuns;
-  const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
-  const int last = combine ? (later ? __ffs(later) - 2 : 31) : lane;
-  const bool leader = combine ? ((heads >> lane) & 1u) != 0 : true;
-  float db[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const float bi = b[i];
-    float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
-    if (combine) {
-      cv.x = run_sum(cv.x, lane, last);
-      cv.y = run_sum(cv.y, lane, last);
-      cv.w = run_sum(cv.w, lane, last);
+  for (int u = 0; u < kVjpPerThread; ++u) {
+    if (q0 + u < total) {
+      fg[u] = __ldg(p.z + e[u]) != 1.0f;
+      nfg += fg[u];
     }
-    if (leader && fg && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
-      atomicAdd(p.d_clip + B.vertex_offset[img] + vid[i], cv);
-    db[i] = fg ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
   }
-  if (a.d_attr_out) {
-    const int K = a.K;
-    const bool vec_rows = (K & 3) == 0;
-    const float* src = a.d_attr_out + e * K;
-    const int64_t aoff = fg ? B.vertex_offset[img] * K : 0;
-    for (int k = 0; k < K; k += 4) {
-      const int n = min(4, K - k);
-      const float4 ga = fg ? load_chunk(src + k, n, vec_rows) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (p.d_bary) {
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float bi = b[i];
-        float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
-        if (combine) av = run_sum4(av, lane, last);
-        const int64_t row = aoff + int64_t(vid[i]) * K + k;
-        if (leader && fg) add_chunk(a.d_attr + row, av, n, vec_rows);
-        if (fg && p.d_bary) {
-          const float4 at = load_chunk(a.attr + row, n, vec_rows);
-          db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
+    for (int u = 0; u < kVjpPerThread; ++u)
+      if (q0 + u < total && !fg[u]) {
+        p.d_bary[3 * e[u]] = 0.0f;
+        p.d_bary[3 * e[u] + 1] = 0.0f;
+        p.d_bary[3 * e[u] + 2] = 0.0f;
+      }
+  }
+  int slot;
+  const int n = block_exclusive_scan<kVjpThreads>(nfg, s_warp, slot);
+  if (n == 0) return;
+#pragma unroll
+  for (int u = 0; u < kVjpPerThread; ++u)
+    if (fg[u]) {
+      s_e[slot] = e[u];
+      s_img[slot] = (unsigned char)img[u];
+      ++slot;
+    }
+  __syncthreads();
+
+  for (int k0 = 0; k0 < n; k0 += kVjpThreads) {
+    const int k = k0 + threadIdx.x;
+    const bool on = k < n;
+    const int im = on ? s_img[k] : 0;
+    const int64_t el = on ? s_e[k] : 0;
+    int id = -1;
+    float b[3] = {0.0f, 0.0f, 0.0f};
+    int vid[3] = {0, 0, 0};
+    float4 V[3];
+    float4 dcl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (on) {
+      id = __ldg(p.ids + el);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) b[i] = __ldg(p.bary + 3 * el + i);
+      const float2 g =
+          p.dvp ? __ldg(reinterpret_cast<const float2*>(p.dvp + el)) : make_float2(0.0f, 0.0f);
+      const int32_t* t = p.tris + 3 * (B.triangle_offset[im] + id);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) vid[i] = __ldg(t + i);
+      const float4* vb = p.clip + B.vertex_offset[im];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) V[i] = __ldg(vb + vid[i]);
+      if (g.x != 0.0f || g.y != 0.0f) {
+        // (c0 b0 + c1 b1) + c2 b2 of the clip coordinates (interpolate.py:24-63);
+        // viewport z carries no gradient (it only enters comparisons).
+        const float4 c = lerp_clip(V[0], V[1], V[2], b);
+        const float W = __int2float_rn(B.width[im]), H = __int2float_rn(B.height[im]);
+        const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
+        dcl = make_float4(dnx / c.w, dny / c.w, 0.0f, -(dnx * c.x + dny * c.y) / (c.w * c.w));
+      }
+    }
+    // Runs of lanes with the same (image, triangle). Warps with many short
+    // runs (small triangles) skip the summation: their atomics rarely
+    // collide.
+    const long long key = on ? (((long long)im << 32) | unsigned(id)) : -1ll;
+    const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
+    const bool combine = __popc(heads) <= kMaxRuns;
+    const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
+    const int last = combine ? (later ? __ffs(later) - 2 : 31) : lane;
+    const bool leader = combine ? ((heads >> lane) & 1u) != 0 : true;
+    float db[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float bi = b[i];
+      float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
+      if (combine) {
+        cv.x = run_sum(cv.x, lane, last);
+        cv.y = run_sum(cv.y, lane, last);
+        cv.w = run_sum(cv.w, lane, last);
+      }
+      if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
+        atomicAdd(p.d_clip + B.vertex_offset[im] + vid[i], cv);
+      db[i] = on ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
+    }
+    if (a.d_attr_out) {
+      const int K = a.K;
+      const bool vec_rows = (K & 3) == 0;
+      const float* src = a.d_attr_out + el * K;
+      const int64_t aoff = on ? B.vertex_offset[im] * K : 0;
+      for (int kk = 0; kk < K; kk += 4) {
+        const int nc = min(4, K - kk);
+        const float4 ga = on ? load_chunk(src + kk, nc, vec_rows) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float bi = b[i];
+          float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
+          if (combine) av = run_sum4(av, lane, last);
+          const int64_t row = aoff + int64_t(vid[i]) * K + kk;
+          if (leader && on) add_chunk(a.d_attr + row, av, nc, vec_rows);
+          if (on && p.d_bary) {
+            const float4 at = load_chunk(a.attr + row, nc, vec_rows);
+            db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
+          }
         }
       }
     }
-  }
-  if (fg && p.d_bary) {
-    p.d_bary[3 * e] = db[0];
-    p.d_bary[3 * e + 1] = db[1];
-    p.d_bary[3 * e + 2] = db[2];
+    if (on && p.d_bary) {
+      p.d_bary[3 * el] = db[0];
+      p.d_bary[3 * el + 1] = db[1];
+      p.d_bary[3 * el + 2] = db[2];
+    }
   }
 }
 
@@ -1004,7 +1049,9 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
     Batch b;
     if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
     const int64_t total = int64_t(L) * b.pix_prefix[cnt];
-    if (total > 0) samples_bwd_kernel<<<unsigned((total + 255) / 256), 256, 0, stream>>>(a, b);
+    if (total > 0)
+      samples_bwd_kernel<<<unsigned((total + kVjpBlock - 1) / kVjpBlock), kVjpThreads, 0,
+                           stream>>>(a, b);
   }
   return launch_status("interpolate + splat positions backward", err);
 }
