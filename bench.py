@@ -209,6 +209,22 @@ def kernel_bytes(wl, fg, C=4, K=4):
   }
 
 
+def max_over_ranks(ms, world, device):
+  """The slowest rank's time: every rank's N replicas must finish a step."""
+  if world <= 1:
+    return ms
+  import torch
+  import torch.distributed as dist
+  t = torch.tensor([ms], dtype=torch.float64, device=device)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t)
+
+
+def whole_job_mpix(world, pixels_per_rank, ms):
+  """Aggregate throughput of N replicas, each rendering its own batch."""
+  return world * pixels_per_rank / ms / 1e3
+
+
 def run_ours(args, rank, world, device):
   import torch
   import torch.distributed as dist
@@ -275,12 +291,7 @@ def run_ours(args, rank, world, device):
       fn()
     e1.record()
     torch.cuda.synchronize(device)
-    ms = e0.elapsed_time(e1) / k
-    if world > 1:
-      t = torch.tensor([ms], device=device)
-      dist.all_reduce(t, op=dist.ReduceOp.MAX)
-      ms = float(t)
-    return ms
+    return max_over_ranks(e0.elapsed_time(e1) / k, world, device)
 
   with ClockSampler(device.index) as clocks:
     clocks.wait_for_samples()
@@ -358,65 +369,79 @@ def run_plain(wl, device, args):
 
 
 # -------------------------------------------------------- CPU (reference)
-def cpu_port_sample(wl, budget_s, threads):
-  """Times the CPU port on images of the workload until `budget_s` of work.
+def cpu_port_sample(wl, budget_s, threads, images=None):
+  """Times the CPU port on images of the workload until `budget_s` of work
+  (or on exactly the given `images`).
 
   Rasterization: the C restatement of the reference CPU rasterizer (float
-  depth semantics), images spread over `threads` host threads. Interpolate,
-  shade, splat, normalize, composite, L2 loss and the backward: torch CPU
-  float32 restatement of the reference's JAX code and torch autograd.
-  Returns (pixels, seconds, images used).
+  depth semantics, single-threaded per image like the reference's), a group
+  of `threads` images at a time on `threads` host threads. Interpolate,
+  shade, splat, normalize, composite, L2 loss and the backward: the torch CPU
+  float32 restatement of the reference's JAX code with torch autograd, on
+  `threads` threads. Returns (pixels, seconds, images used).
   """
+  import concurrent.futures
   import torch
   from oracle import raster, torch_ref
   torch.set_num_threads(threads)
-  order = list(range(len(wl.meshes)))
-  px = 0
-  used = 0
-  t_total = 0.0
-  for i in order:
-    m, cam, (w, h), tgt = wl.meshes[i], wl.cams[i], wl.sizes[i], wl.targets[i]
-    t0 = time.perf_counter()
+  order = list(images) if images is not None else list(range(len(wl.meshes)))
+
+  def rasterize(i):
+    m, cam, (w, h) = wl.meshes[i], wl.cams[i], wl.sizes[i]
     clip = raster.transform(cam, m.vertices)
-    ids, z, b = raster.rasterize(clip, m.triangles, w, h, wl.num_layers, 1,
-                                 raster.DEPTH_FLOAT)
-    state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
-    tc = torch.tensor(clip, requires_grad=True)
-    tcol = torch.tensor(m.colors, requires_grad=True)
-    ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
-    shaded = torch_ref.interpolate(rgba(tcol), ti, tz, tb, tt)
-    out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
-    loss = l2_loss(out, torch.tensor(tgt))
-    torch.autograd.grad(loss, (tc, tcol))
-    t_total += time.perf_counter() - t0
-    px += w * h
-    used += 1
-    if t_total >= budget_s:
-      break
+    return clip, raster.rasterize(clip, m.triangles, w, h, wl.num_layers, 1,
+                                  raster.DEPTH_FLOAT)
+
+  px = used = 0
+  t_total = 0.0
+  with concurrent.futures.ThreadPoolExecutor(threads) as pool:
+    for g0 in range(0, len(order), threads):
+      group = order[g0:g0 + threads]
+      t0 = time.perf_counter()
+      rasters = list(pool.map(rasterize, group))  # ctypes calls release the GIL
+      for i, (clip, (ids, z, b)) in zip(group, rasters):
+        m, (w, h), tgt = wl.meshes[i], wl.sizes[i], wl.targets[i]
+        state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
+        tc = torch.tensor(clip, requires_grad=True)
+        tcol = torch.tensor(m.colors, requires_grad=True)
+        ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
+        shaded = torch_ref.interpolate(rgba(tcol), ti, tz, tb, tt)
+        out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
+        loss = l2_loss(out, torch.tensor(tgt))
+        torch.autograd.grad(loss, (tc, tcol))
+        px += w * h
+        used += 1
+      t_total += time.perf_counter() - t0
+      if images is None and t_total >= budget_s:
+        break
   return px, t_total, used
 
 
 def run_reference(args):
+  """The reference arm: the CPU port of the reference's path (see
+  cpu_port_sample) on the machine's host cores. Step i renders image i mod N of
+  the workload forward and backward; the value is the timed steps' pixels
+  over their time."""
   wl = Workload(args.workload, args.num_meshes)
   threads = os.cpu_count() or 1
-  # Images are processed one after another, each op using all host threads.
-  vals = []
-  sample = None
+  n = len(wl.meshes)
+  px_t = secs_t = 0.0
   for it in range(args.warmup + args.steps):
-    px, secs, used = cpu_port_sample(wl, args.cpu_budget / max(1, args.steps), threads)
+    px, secs, _ = cpu_port_sample(wl, 0.0, threads, images=[it % n])
     if it >= args.warmup:
-      vals.append(px / secs / 1e6)
-      sample = "first %d of %d images (%d px) per step" % (used, len(wl.meshes), px)
-  value = float(np.median(vals))
+      px_t += px
+      secs_t += secs
+  value = px_t / secs_t / 1e6
+  sample = ("one image per step (images %d..%d of %d, cycling), %d px in %.1f s"
+            % (args.warmup % n, (args.warmup + args.steps - 1) % n, n, px_t, secs_t))
   line = {
       "metric": "RtS fwd+bwd Mpix/s on 1 GB300, batched vs plain, at 1e-5 rel err",
       "value": value, "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps,
-      "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-      "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-      "impl": "reference",
-      "config": {"workload": wl.desc, "num_images": len(wl.meshes),
-                 "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
-                 "num_layers": wl.num_layers},
+      "warmup": args.warmup, "ms_per_step": secs_t * 1e3 / args.steps,
+      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (seeded meshes, cameras and targets)", "impl": "reference",
+      "config": {"workload": wl.desc, "num_images": n, "total_mpix": wl.pixels / 1e6,
+                 "total_triangles": wl.triangles, "num_layers": wl.num_layers},
       "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "port",
                        "sample": sample},
       "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
@@ -457,7 +482,8 @@ def main():
     threads = os.cpu_count() or 1
     px, secs, used = cpu_port_sample(wl, args.cpu_budget, threads)
     cpu = {"value": px / secs / 1e6, "unit": "Mpix/s", "cores": threads, "kind": "port",
-           "sample": "first %d of %d images of the workload (%d px), fwd+bwd, %.1f s"
+           "sample": "first %d of %d images of the workload (%d px), fwd+bwd, %.1f s; "
+                     "rasterizer one image per thread, splat on all threads"
                      % (used, len(wl.meshes), px, secs)}
   if rank != 0:
     if world > 1:
@@ -468,7 +494,7 @@ def main():
   nbytes = kernel_bytes(wl, res["fg"])
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
-  value = world * wl.pixels / res["ms"] / 1e3
+  value = whole_job_mpix(world, wl.pixels, res["ms"])
   line = {
       "metric": "RtS fwd+bwd Mpix/s on 1 GB300, batched vs plain, at 1e-5 rel err",
       "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
@@ -481,7 +507,7 @@ def main():
                  "foreground_samples": res["fg"], "parallelism": "replicas" if world > 1 else "1 GPU",
                  "l2": "per-step working set of several GB > 129 MB L2",
                  "cuda_graph": True, "raster_tile_autotuned": res["tile"]},
-      "e2e": {"value": world * wl.pixels / res["ms_e2e"] / 1e3, "unit": "Mpix/s",
+      "e2e": {"value": whole_job_mpix(world, wl.pixels, res["ms_e2e"]), "unit": "Mpix/s",
               "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
       "plain": None if res["plain"] is None else {
           "value": res["plain"]["value"], "unit": "Mpix/s",
