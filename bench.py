@@ -185,23 +185,37 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- our arm
-def kernel_bytes(wl, fg, C=4, K=4):
+# DRAM bytes (read + write) per layer sample of each op, from the ncu
+# capture of the 8-mesh subset of the ragged workload
+# (profiles/*_ragged8_subset.md): setup + tile scan + binning + fine raster;
+# splat forward; splat backward; samples VJP. Traffic grows with the layer
+# samples, so the full workload's traffic is this times its samples.
+TRAFFIC_PER_SAMPLE = {"raster": 40.15, "splat_fwd": 24.76, "splat_bwd": 43.48,
+                      "samples_bwd": 18.56}
+
+
+def kernel_bytes(wl, fg, near=None, C=4, K=4):
   """Algorithmic (compulsory) HBM bytes per launch of each kernel: every
   input read and every output written once. `fg` = foreground layer samples
-  among the L * P; work on background samples stops after their depth."""
+  among the L * P; work on background samples stops after their depth.
+  `near` = pixels within one pixel of a foreground sample (the only ones
+  whose splat accumulators the backward needs); all pixels if None."""
   L, P, T, V = wl.num_layers, wl.pixels, wl.triangles, wl.vertices
   S = L * P
+  near = P if near is None else near
   return {
       # rasterizer with the fused interpolation epilogue: the mesh (indices,
-      # clip vertices, attributes) in; ids, z, bary, K attributes and the
-      # viewport position of every sample out
-      "raster": T * 12 + V * (16 + 4 * K) + S * (20 + 4 * K + 16),
-      # position of every sample and color of every foreground sample in;
-      # composited color and saved accumulators (3 (C + 1)) per pixel out
-      "splat_fwd": 16 * S + 4 * C * fg + P * (4 * C + 12 * (C + 1)),
-      # saved accumulators and d color per pixel, position of every sample,
-      # color of the foreground ones in; d color and d position per sample out
-      "splat_bwd": P * (12 * (C + 1) + 4 * C) + 16 * S + 4 * C * fg + S * (4 * C + 16),
+      # clip vertices, attributes) in; ids, z, bary and K attributes of
+      # every sample and the viewport position of every foreground sample out
+      "raster": T * 12 + V * (16 + 4 * K) + S * (20 + 4 * K) + 16 * fg,
+      # depth of every sample, position and color of every foreground
+      # sample in; composited color and saved accumulators (3 (C + 1)) per
+      # pixel out
+      "splat_fwd": 4 * S + (16 + 4 * C) * fg + 4 * C * P + 12 * (C + 1) * near,
+      # saved accumulators and d color per pixel, depth of every sample,
+      # position and color of the foreground ones in; d color of every
+      # sample and d position of every foreground sample out
+      "splat_bwd": near * (12 * (C + 1) + 4 * C) + 4 * S + (16 + 4 * C) * fg + 4 * C * S + 16 * fg,
       # z of every sample; ids, bary, d position and d attributes of the
       # foreground ones and the mesh in; vertex gradients (clip + attributes)
       # read and written once
@@ -268,10 +282,15 @@ def run_ours(args, rank, world, device):
   step()
   torch.cuda.synchronize(device)
   launches_per_step = kernels.LAUNCHES.count
-  # Foreground layer samples of the workload (for the algorithmic bytes).
+  # Foreground layer samples of the workload, and pixels within one pixel
+  # of one (for the algorithmic bytes).
   with torch.no_grad():
     _, z_fg, _ = r.rasterize(kernels.transform(verts, cams, r.batch))
     fg = int((z_fg != 1.0).sum())
+    near = 0
+    for i in range(r.batch.n):
+      m = (r.batch.layered_view(z_fg, i, wl.num_layers) != 1.0).any(0).float()
+      near += int(torch.nn.functional.max_pool2d(m[None, None], 3, 1, 1).sum())
   del z_fg
   graph = torch.cuda.CUDAGraph()
   with torch.cuda.graph(graph):
@@ -327,7 +346,7 @@ def run_ours(args, rank, world, device):
   if not args.no_plain and rank == 0:
     plain = run_plain(wl, device, args)
   tile = [r.config.tile_width, r.config.tile_height, r.config.large_tiles]
-  return dict(wl=wl, fg=fg, tile=tile, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
+  return dict(wl=wl, fg=fg, near=near, tile=tile, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
               loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
               plain=plain, renderer=r)
 
@@ -491,7 +510,7 @@ def main():
     return
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
-  nbytes = kernel_bytes(wl, res["fg"])
+  nbytes = kernel_bytes(wl, res["fg"], res["near"])
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
   value = whole_job_mpix(world, wl.pixels, res["ms"])
@@ -504,7 +523,8 @@ def main():
       "config": {"workload": wl.desc, "num_images": len(wl.meshes),
                  "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
                  "num_layers": wl.num_layers,
-                 "foreground_samples": res["fg"], "parallelism": "replicas" if world > 1 else "1 GPU",
+                 "foreground_samples": res["fg"], "pixels_near_foreground": res["near"],
+                 "parallelism": "replicas" if world > 1 else "1 GPU",
                  "l2": "per-step working set of several GB > 129 MB L2",
                  "cuda_graph": True, "raster_tile_autotuned": res["tile"]},
       "e2e": {"value": whole_job_mpix(world, wl.pixels, res["ms_e2e"]), "unit": "Mpix/s",
@@ -522,7 +542,11 @@ def main():
           "mtriangles_per_s": wl.triangles / (pk["raster"] * 1e-3) / 1e6},
       "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
                    "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                   "algorithmic_bytes": nbytes[dom], "traffic": None},
+                   "algorithmic_bytes": nbytes[dom],
+                   "traffic": (TRAFFIC_PER_SAMPLE[dom] * wl.num_layers * wl.pixels
+                               if dom in TRAFFIC_PER_SAMPLE else None),
+                   "traffic_source": "ncu DRAM bytes of the 8-mesh subset, scaled by "
+                                     "layer samples"},
       "cpu_baseline": cpu,
       "clocks": res["clock"],
       "loss": res["loss"],
