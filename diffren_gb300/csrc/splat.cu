@@ -530,13 +530,15 @@ __device__ __forceinline__ void accumulate(float2 (&acc)[2 * Q], float& wacc, co
 // the per-tap surface test, normalizes, composites and stores. Background
 // samples weigh nothing, so their weights and colors are never written or
 // read, and a tile whose region holds no foreground sample writes zeros.
-template <int C>
+// LT > 0 fixes the layer count at compile time (the common L = 3 case), so
+// the layer loops unroll; LT = 0 reads it from the arguments.
+template <int C, int LT>
 __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArgs a, Batch B) {
   constexpr int Q = Groups<C>::Q;
   extern __shared__ __align__(16) float smem[];
   __shared__ unsigned s_layers;
   const TileRef tr = tile_of(B);
-  const int L = a.L;
+  const int L = LT > 0 ? LT : a.L;
   float* zs = smem;
   float* wx = zs + L * kRR;
   float* wy = wx + 3 * L * kRR;
@@ -743,12 +745,12 @@ __device__ __forceinline__ void accum_adjoint(const float acc[3][C], const float
 // layer's depth z[l][i]; each sample of the tile then reads those of the 9
 // pixels it reached, in the class its surface test picked, and writes
 // d color and d viewport xy. No atomics.
-template <int C>
+template <int C, int LT>
 __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B) {
   constexpr int Q = Groups<C>::Q;
   extern __shared__ __align__(16) float smem[];
   const TileRef tr = tile_of(B);
-  const int L = a.L;
+  const int L = LT > 0 ? LT : a.L;
   const int W = B.width[tr.img], H = B.height[tr.img];
   const int64_t HW = int64_t(W) * H;
   float* zs = smem;
@@ -908,11 +910,11 @@ size_t bwd_smem(int L, int C) {
   return size_t(L + 3 * 4 * ((C + 3) / 4) + 3) * kRR * 4;
 }
 
-template <int C>
+template <int C, int LT>
 int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
               cudaStream_t stream, std::string& err) {
   const size_t smem = bwd ? bwd_smem(a.L, C) : fwd_smem(a.L, C);
-  auto kern = bwd ? splat_bwd_kernel<C> : splat_fwd_kernel<C>;
+  auto kern = bwd ? splat_bwd_kernel<C, LT> : splat_fwd_kernel<C, LT>;
   // Raise the dynamic shared-memory limit once per kernel and size (host-side
   // attribute only; later calls skip it).
   static size_t reserved[2] = {0, 0};
@@ -936,15 +938,17 @@ int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
 
 int dispatch(bool bwd, int C, const SplatArgs& a, const dr_image_desc* images, int n,
              cudaStream_t stream, std::string& err) {
+  if (C == 4 && a.L == 3) return run_splat<4, 3>(bwd, a, images, n, stream, err);
+  if (C == 4 && a.L == 1) return run_splat<4, 1>(bwd, a, images, n, stream, err);
   switch (C) {
-    case 1: return run_splat<1>(bwd, a, images, n, stream, err);
-    case 2: return run_splat<2>(bwd, a, images, n, stream, err);
-    case 3: return run_splat<3>(bwd, a, images, n, stream, err);
-    case 4: return run_splat<4>(bwd, a, images, n, stream, err);
-    case 5: return run_splat<5>(bwd, a, images, n, stream, err);
-    case 6: return run_splat<6>(bwd, a, images, n, stream, err);
-    case 7: return run_splat<7>(bwd, a, images, n, stream, err);
-    case 8: return run_splat<8>(bwd, a, images, n, stream, err);
+    case 1: return run_splat<1, 0>(bwd, a, images, n, stream, err);
+    case 2: return run_splat<2, 0>(bwd, a, images, n, stream, err);
+    case 3: return run_splat<3, 0>(bwd, a, images, n, stream, err);
+    case 4: return run_splat<4, 0>(bwd, a, images, n, stream, err);
+    case 5: return run_splat<5, 0>(bwd, a, images, n, stream, err);
+    case 6: return run_splat<6, 0>(bwd, a, images, n, stream, err);
+    case 7: return run_splat<7, 0>(bwd, a, images, n, stream, err);
+    case 8: return run_splat<8, 0>(bwd, a, images, n, stream, err);
     default:
       err = "splat supports 1 to 8 channels";
       return DR_ERR_INVALID_ARGUMENT;
