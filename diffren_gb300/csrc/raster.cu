@@ -277,14 +277,15 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
 }
 
 // kFused adds the sample outputs to the epilogue; it needs more registers,
-// so it is a separate instantiation with its own occupancy.
-template <bool kFused>
+// so it is a separate instantiation with its own occupancy. LT > 0 fixes the
+// layer count at compile time (the common L = 3), LT = 0 reads it.
+template <bool kFused, int LT>
 __global__ void __launch_bounds__(kThreads, kFused ? 4 : 5) fine_raster_kernel(RasterArgs a,
                                                                              Batch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_warp[kThreads / 32];
   __shared__ int s_item;
-  const int TW = a.TW, TH = a.TH, TP = TW * TH, L = a.L;
+  const int TW = a.TW, TH = a.TH, TP = TW * TH, L = LT > 0 ? LT : a.L;
   FineSmem s;
   {
     unsigned char* p = smem_raw;
@@ -508,12 +509,12 @@ __global__ void depth_codec_selftest_kernel(unsigned long long* out) {
 // Raises the fine rasterizer's dynamic shared-memory limit and computes its
 // persistent grid (resident blocks per SM x SMs), once per instantiation
 // and shared-memory size (host-side attributes only).
-template <bool kFused>
+template <bool kFused, int LT>
 bool prepare_fine(size_t smem, int& sms, int& per_sm, std::string& err) {
   static size_t smem_set = 0, occ_smem = 0;
   static int s_sms = 0, s_per_sm = 0;
   if (smem > 48 * 1024 && smem > smem_set) {
-    if (cudaFuncSetAttribute(fine_raster_kernel<kFused>,
+    if (cudaFuncSetAttribute(fine_raster_kernel<kFused, LT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem)) != cudaSuccess) {
       err = "tile and layer count need more shared memory than the device has";
@@ -525,7 +526,7 @@ bool prepare_fine(size_t smem, int& sms, int& per_sm, std::string& err) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&s_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per_sm, fine_raster_kernel<kFused>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per_sm, fine_raster_kernel<kFused, LT>,
                                                   kThreads, smem);
     if (s_per_sm < 1) s_per_sm = 1;
     occ_smem = smem;
@@ -625,10 +626,16 @@ int raster_launch(const float* vertices, const int32_t* triangles,
   }
   const size_t smem = fine_smem_bytes(L, TW, TH);
   const bool fused = so.positions != nullptr;
+  // Instantiations: fused or not, three layers or any.
+  using Fine = void (*)(RasterArgs, Batch);
+  using Prep = bool (*)(size_t, int&, int&, std::string&);
+  const int variant = (fused ? 2 : 0) + (L == 3 ? 1 : 0);
+  const Fine fine[4] = {fine_raster_kernel<false, 0>, fine_raster_kernel<false, 3>,
+                        fine_raster_kernel<true, 0>, fine_raster_kernel<true, 3>};
+  const Prep prep[4] = {prepare_fine<false, 0>, prepare_fine<false, 3>,
+                        prepare_fine<true, 0>, prepare_fine<true, 3>};
   int sms = 0, per_sm = 0;
-  if (!(fused ? prepare_fine<true>(smem, sms, per_sm, err)
-              : prepare_fine<false>(smem, sms, per_sm, err)))
-    return DR_ERR_INVALID_ARGUMENT;
+  if (!prep[variant](smem, sms, per_sm, err)) return DR_ERR_INVALID_ARGUMENT;
 
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
     const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
@@ -678,10 +685,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
       bin_scatter_kernel<<<grid, 256, 0, stream>>>(a, b);
     }
     const int blocks = std::max(1, std::min(tiles, sms * per_sm));
-    if (fused)
-      fine_raster_kernel<true><<<blocks, kThreads, smem, stream>>>(a, b);
-    else
-      fine_raster_kernel<false><<<blocks, kThreads, smem, stream>>>(a, b);
+    fine[variant]<<<blocks, kThreads, smem, stream>>>(a, b);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       err = std::string("raster launch failed: ") + cudaGetErrorString(e);
