@@ -48,7 +48,7 @@ SIGNATURES = {
     "dr_rasterize_batch_workspace_bytes": (_S, [_P, _I, _P]),
     "dr_rasterize_batch": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _S, _P]),
     "dr_rasterize_batch_interpolate": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P,
-                                           _P, _S, _P]),
+                                           _P, _P, _S, _P]),
     "dr_rasterize_triangles_workspace_bytes": (_S, [_I, _I, _I, _I]),
     "dr_rasterize_triangles": (_I, [_P, _I, _P, _I, _I, _I, _I, _I, _I, _P, _P,
                                     _P, _P, _S, _P]),
@@ -65,8 +65,8 @@ SIGNATURES = {
     "dr_diff_barycentrics_bwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_interpolate_with_positions_fwd": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I, _I,
                                               _P, _P, _P]),
-    "dr_interpolate_with_positions_bwd": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P,
-                                              _I, _I, _P, _P, _P, _P]),
+    "dr_interpolate_with_positions_bwd": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _P,
+                                              _P, _I, _I, _P, _P, _P, _P]),
     "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),

@@ -79,11 +79,12 @@ int dr_rasterize_batch_interpolate(const float* vertices, const int32_t* triangl
                                    const dr_raster_config* config, int32_t* triangle_ids,
                                    float* z_buffer, float* barycentrics,
                                    const float* attributes, int32_t num_channels,
-                                   float* attributes_out, float* positions, void* workspace,
+                                   float* attributes_out, float* positions,
+                                   int32_t* vertex_ids, void* workspace,
                                    size_t workspace_bytes, void* stream) {
   std::string err;
   dr::SampleOutputs so{attributes, num_channels, attributes_out,
-                       reinterpret_cast<float4*>(positions)};
+                       reinterpret_cast<float4*>(positions), vertex_ids};
   return finish(dr::raster_launch(vertices, triangles, images, num_images, config,
                                   triangle_ids, z_buffer, barycentrics, workspace,
                                   workspace_bytes, as_stream(stream), err, &so),
@@ -223,6 +224,7 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       int32_t num_channels, const float* clip_vertices,
                                       const int32_t* triangles, const int32_t* triangle_ids,
                                       const float* z_buffer, const float* barycentrics,
+                                      const float* positions, const int32_t* vertex_ids,
                                       const dr_image_desc* images, int32_t num_images,
                                       int32_t num_layers, float* d_attributes,
                                       float* d_clip_vertices, float* d_barycentrics,
@@ -230,10 +232,10 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
   std::string err;
   return finish(dr::samples_bwd_launch(d_attributes_out, d_positions, attributes,
                                        num_channels, clip_vertices, triangles,
-                                       triangle_ids, z_buffer, barycentrics, images,
-                                       num_images, num_layers, d_attributes,
-                                       d_clip_vertices, d_barycentrics, as_stream(stream),
-                                       err),
+                                       triangle_ids, z_buffer, barycentrics, positions,
+                                       vertex_ids, images, num_images, num_layers,
+                                       d_attributes, d_clip_vertices, d_barycentrics,
+                                       as_stream(stream), err),
                 err);
 }
 

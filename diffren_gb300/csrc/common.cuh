@@ -83,7 +83,8 @@ struct SampleOutputs {
   const float* attr;  // [V, K] packed per mesh (nullable)
   int K;
   float* attr_out;    // [L * P, K]
-  float4* positions;  // [L * P]; null = no fused outputs
+  float4* positions;  // [L * P] viewport xyz + clip w; null = no fused outputs
+  int32_t* vertex_ids;  // [L * P, 3] (nullable)
 };
 
 // ------------------------------------------------------- sample helpers

@@ -110,8 +110,9 @@ int samples_fwd_launch(const float* attributes, int K, const float* clip,
 int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
                        const float* attributes, int K, const float* clip,
                        const int32_t* tris, const int32_t* ids, const float* z,
-                       const float* bary, const dr_image_desc* images, int n, int L,
-                       float* d_attributes, float* d_clip, float* d_bary,
+                       const float* bary, const float* positions,
+                       const int32_t* vertex_ids, const dr_image_desc* images, int n,
+                       int L, float* d_attributes, float* d_clip, float* d_bary,
                        cudaStream_t stream, std::string& err);
 int positions_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
                          const float* z, const float* bary, const dr_image_desc* images,

@@ -235,9 +235,10 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 // large and small triangles cost the same per pixel.
 // Fused interpolation of one layer sample o with triangle `id` and the
 // barycentrics just written: the splat position of a foreground sample
-// (splat.py:207-221) and, when requested, the attributes (interpolate.py:24-63,
-// background 0). The same operations, in the same order, as
-// samples_fwd_kernel on the stored buffers.
+// (splat.py:207-221) with its clip w, its three vertex indices when
+// requested (the Framebuffer's vertex_ids, rasterize.py:111-113), and the
+// attributes (interpolate.py:24-63, background 0). The same operations, in
+// the same order, as samples_fwd_kernel on the stored buffers.
 __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B, int img, int id,
                                           float zz, const float b[3], int64_t o) {
   const SampleOutputs& so = a.so;
@@ -266,8 +267,16 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
                     n, vec_rows);
       }
     }
+    // w carries the interpolated clip w, which the VJP needs (background
+    // and foreground are told apart by the depth buffer).
     so.positions[o] = viewport_of(c, __int2float_rn(B.width[img]),
-                                  __int2float_rn(B.height[img]), 1.0f);
+                                  __int2float_rn(B.height[img]), c.w);
+    if (so.vertex_ids) {
+      int32_t* vo = so.vertex_ids + 3 * o;
+      vo[0] = v0;
+      vo[1] = v1;
+      vo[2] = v2;
+    }
   } else if (ao) {
     // Background: attributes 0; the position is left unwritten (consumers
     // take background samples from the depth buffer).

@@ -151,6 +151,8 @@ __global__ void __launch_bounds__(256) positions_bwd_kernel(PosArgs a, Batch B) 
 // paths use it; results equal interp_fwd_kernel and positions_fwd_kernel.
 struct SampleArgs {
   PosArgs pos;
+  const float4* vp;    // backward: stored positions, w = clip w (nullable)
+  const int32_t* vid;  // backward: stored vertex indices [L*P, 3] (nullable)
   const float* attr;  // [V, K]
   int K;
   float* attr_out;         // [L*P, K]
@@ -297,35 +299,61 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
     int id = -1;
     float b[3] = {0.0f, 0.0f, 0.0f};
     int vid[3] = {0, 0, 0};
-    float4 V[3];
+    float4 V[3] = {make_float4(0.0f, 0.0f, 0.0f, 1.0f), make_float4(0.0f, 0.0f, 0.0f, 1.0f),
+                   make_float4(0.0f, 0.0f, 0.0f, 1.0f)};
     float4 dcl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (on) {
-      id = __ldg(p.ids + el);
 #pragma unroll
       for (int i = 0; i < 3; ++i) b[i] = __ldg(p.bary + 3 * el + i);
       const float2 g =
           p.dvp ? __ldg(reinterpret_cast<const float2*>(p.dvp + el)) : make_float2(0.0f, 0.0f);
-      const int32_t* t = p.tris + 3 * (B.triangle_offset[im] + id);
+      if (a.vid) {
+        // Vertex indices stored by the rasterizer: no triangle gather.
 #pragma unroll
-      for (int i = 0; i < 3; ++i) vid[i] = __ldg(t + i);
-      const float4* vb = p.clip + B.vertex_offset[im];
+        for (int i = 0; i < 3; ++i) vid[i] = __ldg(a.vid + 3 * el + i);
+        id = vid[0];
+      } else {
+        id = __ldg(p.ids + el);
+        const int32_t* t = p.tris + 3 * (B.triangle_offset[im] + id);
 #pragma unroll
-      for (int i = 0; i < 3; ++i) V[i] = __ldg(vb + vid[i]);
-      if (g.x != 0.0f || g.y != 0.0f) {
-        // (c0 b0 + c1 b1) + c2 b2 of the clip coordinates (interpolate.py:24-63);
-        // viewport z carries no gradient (it only enters comparisons).
-        const float4 c = lerp_clip(V[0], V[1], V[2], b);
-        const float W = __int2float_rn(B.width[im]), H = __int2float_rn(B.height[im]);
-        const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
-        dcl = make_float4(dnx / c.w, dny / c.w, 0.0f, -(dnx * c.x + dny * c.y) / (c.w * c.w));
+        for (int i = 0; i < 3; ++i) vid[i] = __ldg(t + i);
+      }
+      const float W = __int2float_rn(B.width[im]), H = __int2float_rn(B.height[im]);
+      const float dnx = g.x * W * 0.5f, dny = g.y * H * 0.5f;
+      const bool moved = g.x != 0.0f || g.y != 0.0f;
+      if (a.vp && !p.d_bary) {
+        // From the stored position: ndc = 2 viewport / (W, H) - 1, and the
+        // clip w it carries (no vertex gathers).
+        if (moved) {
+          const float4 q = __ldg(a.vp + el);
+          const float nx = q.x * (2.0f / W) - 1.0f, ny = q.y * (2.0f / H) - 1.0f;
+          dcl = make_float4(dnx / q.w, dny / q.w, 0.0f, -(dnx * nx + dny * ny) / q.w);
+        }
+      } else {
+        const float4* vb = p.clip + B.vertex_offset[im];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) V[i] = __ldg(vb + vid[i]);
+        if (moved) {
+          // (c0 b0 + c1 b1) + c2 b2 of the clip coordinates
+          // (interpolate.py:24-63); viewport z carries no gradient (it only
+          // enters comparisons).
+          const float4 c = lerp_clip(V[0], V[1], V[2], b);
+          dcl = make_float4(dnx / c.w, dny / c.w, 0.0f, -(dnx * c.x + dny * c.y) / (c.w * c.w));
+        }
       }
     }
-    // Runs of lanes with the same (image, triangle). Warps with many short
-    // runs (small triangles) skip the summation: their atomics rarely
-    // collide.
-    const long long key = on ? (((long long)im << 32) | unsigned(id)) : -1ll;
-    const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
+    // Runs of lanes with the same image and the same three vertex rows.
+    // Warps with many short runs (small triangles) skip the summation:
+    // their atomics rarely collide.
+    // (All four shuffles run on every lane before any comparison.)
+    const int kim = on ? im : -1;
+    const int p_im = __shfl_up_sync(0xffffffffu, kim, 1);
+    const int p_v0 = __shfl_up_sync(0xffffffffu, vid[0], 1);
+    const int p_v1 = __shfl_up_sync(0xffffffffu, vid[1], 1);
+    const int p_v2 = __shfl_up_sync(0xffffffffu, vid[2], 1);
+    const bool differs = (kim != p_im) | (vid[0] != p_v0) | (vid[1] != p_v1) | (vid[2] != p_v2);
+    (void)id;
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || differs);
     const bool combine = __popc(heads) <= kMaxRuns;
     const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
     const int last = combine ? (later ? __ffs(later) - 2 : 31) : lane;
@@ -415,18 +443,26 @@ struct Taps {
   float d0, d1;
 };
 
-__device__ __forceinline__ Taps taps_of(float4 q, float coef) {
+// `fg` is the foreground weight of the sample (the mask value; 1 for
+// positions from the rasterizer, whose w holds the clip w instead).
+__device__ __forceinline__ Taps taps_of(float4 q, float fg, float coef) {
   Taps t;
   t.d0 = __fsub_rn(__fadd_rn(floorf(q.x), 0.5f), q.x);
   t.d1 = __fsub_rn(__fadd_rn(floorf(q.y), 0.5f), q.y);
-  const float fc = __fmul_rn(q.w, coef);
+  const float fc = __fmul_rn(fg, coef);
 #pragma unroll
   for (int u = 0; u < 3; ++u) {
     const float dx = __fadd_rn(t.d0, float(u - 1)), dy = __fadd_rn(t.d1, float(u - 1));
-    t.ex[u] = q.w != 0.0f ? __fmul_rn(fc, __expf(__fmul_rn(-2.0f, __fmul_rn(dx, dx)))) : 0.0f;
-    t.ey[u] = q.w != 0.0f ? __expf(__fmul_rn(-2.0f, __fmul_rn(dy, dy))) : 0.0f;
+    t.ex[u] = fg != 0.0f ? __fmul_rn(fc, __expf(__fmul_rn(-2.0f, __fmul_rn(dx, dx)))) : 0.0f;
+    t.ey[u] = fg != 0.0f ? __expf(__fmul_rn(-2.0f, __fmul_rn(dy, dy))) : 0.0f;
   }
   return t;
+}
+
+// Foreground weight of a loaded sample: from the depth buffer when there is
+// one (the position's w is then the clip w), else the position's w.
+__device__ __forceinline__ float fg_weight(bool zb, bool fg_bit, float4 q) {
+  return zb ? (fg_bit ? 1.0f : 0.0f) : q.w;
 }
 
 template <int C>
@@ -568,9 +604,10 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
         float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
         if (in && (!a.zb || ((m >> l) & 1u))) q = __ldg(a.vp + e0 + l * HW);
         zs[l * kRR + i] = q.z;
-        if (q.w != 0.0f) {
+        const float fgw = fg_weight(a.zb != nullptr, in && ((m >> l) & 1u), q);
+        if (fgw != 0.0f) {
           m |= 1u << l;
-          const Taps t = taps_of(q, a.coef);
+          const Taps t = taps_of(q, fgw, a.coef);
 #pragma unroll
           for (int u = 0; u < 3; ++u) {
             wx[(l * 3 + u) * kRR + i] = t.ex[u];
@@ -852,8 +889,9 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
 #pragma unroll
     for (int hh = 0; hh < 2 * Q; ++hh) dcol[hh] = make_float2(0.0f, 0.0f);
     float dvx = 0.0f, dvy = 0.0f;
-    if (q.w != 0.0f) {
-      const Taps t = taps_of(q, a.coef);
+    const float fgw = fg_weight(a.zb != nullptr, (own >> l) & 1u, q);
+    if (fgw != 0.0f) {
+      const Taps t = taps_of(q, fgw, a.coef);
       float4 col[Q];
       load_groups<C>(a.colors + e * C, col);
 #pragma unroll
@@ -887,7 +925,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
       dc[2 * hh + 1] = dcol[hh].y;
     }
     store_row<C>(a.d_colors + e * C, dc);
-    if (q.w != 0.0f || !a.zb) a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
+    if (fgw != 0.0f || !a.zb) a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
   }
 }
 
@@ -1024,8 +1062,9 @@ int samples_fwd_launch(const float* attributes, int K, const float* clip,
 int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
                        const float* attributes, int K, const float* clip,
                        const int32_t* tris, const int32_t* ids, const float* z,
-                       const float* bary, const dr_image_desc* images, int n, int L,
-                       float* d_attributes, float* d_clip, float* d_bary,
+                       const float* bary, const float* positions,
+                       const int32_t* vertex_ids, const dr_image_desc* images, int n,
+                       int L, float* d_attributes, float* d_clip, float* d_bary,
                        cudaStream_t stream, std::string& err) {
   int rc;
   if (!check_batch(L, n, images, err, rc)) return rc;
@@ -1034,15 +1073,17 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
     err = "d_clip_vertices (and d_attributes with d_attr_out) must be non-null";
     return DR_ERR_INVALID_ARGUMENT;
   }
-  if (!aligned16({d_positions, clip, d_clip}) ||
+  if (!aligned16({d_positions, clip, d_clip, positions}) ||
       (K % 4 == 0 && !aligned16({d_attr_out, attributes, d_attributes}))) {
-    err = "d_positions, clip_vertices, d_clip_vertices (and, with a multiple of 4 "
-          "channels, the attribute buffers) must be 16-byte aligned";
+    err = "d_positions, clip_vertices, d_clip_vertices, positions (and, with a multiple "
+          "of 4 channels, the attribute buffers) must be 16-byte aligned";
     return DR_ERR_MISALIGNED;
   }
   SampleArgs a{};
   a.pos.clip = reinterpret_cast<const float4*>(clip);
   a.pos.tris = tris; a.pos.ids = ids; a.pos.z = z; a.pos.bary = bary; a.pos.L = L;
+  a.vp = reinterpret_cast<const float4*>(positions);
+  a.vid = vertex_ids;
   a.pos.dvp = reinterpret_cast<const float4*>(d_positions);
   a.pos.d_clip = reinterpret_cast<float4*>(d_clip);
   a.pos.d_bary = d_bary;

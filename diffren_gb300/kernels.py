@@ -409,14 +409,18 @@ class _Samples(torch.autograd.Function):
   def backward(ctx, d_out, d_vp):
     attributes, clip, bary, triangles, ids, z = ctx.saved_tensors
     d_attr, d_clip, d_bary = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary,
-                                          triangles, ids, z, ctx.needs_input_grad[2])
+                                          triangles, ids, z, ctx.needs_input_grad[2],
+                                          None, None)
     return (d_attr if ctx.needs_input_grad[0] else None,
             d_clip if ctx.needs_input_grad[1] else None,
             d_bary, None, None, None, None, None)
 
 
-def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, want_bary):
-  """(d attributes, d clip, d barycentrics or None) of the fused pass."""
+def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, want_bary,
+                 positions, vertex_ids):
+  """(d attributes, d clip, d barycentrics or None) of the fused pass;
+  `positions` (w = clip w) and `vertex_ids` from the fused rasterizer, or
+  None."""
   lib = _lib.load()
   if d_out is None and d_vp is None:
     return None, None, None
@@ -432,8 +436,9 @@ def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, wa
   with _op("samples_bwd", _groups(ctx.batch)):
     rc = lib.dr_interpolate_with_positions_bwd(
         _p(d_out), _p(d_vp), _p(attributes), attributes.shape[1], _p(clip),
-        _p(triangles), _p(ids), _p(z), _p(bary), ctx.batch.ptr, ctx.batch.n, ctx.L,
-        _p(d_attr), _p(d_clip), _p(d_bary), _stream(clip.device))
+        _p(triangles), _p(ids), _p(z), _p(bary), _p(positions), _p(vertex_ids),
+        ctx.batch.ptr, ctx.batch.n, ctx.L, _p(d_attr), _p(d_clip), _p(d_bary),
+        _stream(clip.device))
   _lib.check(rc, "dr_interpolate_with_positions_bwd")
   return d_attr, d_clip, d_bary
 
@@ -455,13 +460,15 @@ class _RasterSamples(torch.autograd.Function):
     bary = torch.empty(n, 3, dtype=torch.float32, device=dev)
     out = torch.empty(n, K, dtype=torch.float32, device=dev)
     vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
+    vids = torch.empty(n, 3, dtype=torch.int32, device=dev)
     ws = workspace.get(raster_workspace_bytes(batch, config))
     with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
       rc = lib.dr_rasterize_batch_interpolate(
           _p(clip), _p(triangles), batch.ptr, batch.n, ctypes.byref(config), _p(ids), _p(z),
-          _p(bary), _p(attributes), K, _p(out), _p(vp), _p(ws), ws.numel(), _stream(dev))
+          _p(bary), _p(attributes), K, _p(out), _p(vp), _p(vids), _p(ws), ws.numel(),
+          _stream(dev))
     _lib.check(rc, "dr_rasterize_batch_interpolate")
-    ctx.save_for_backward(attributes, clip, bary, triangles, ids, z)
+    ctx.save_for_backward(attributes, clip, bary, triangles, ids, z, vp, vids)
     ctx.batch, ctx.L = batch, L
     ctx.set_materialize_grads(False)
     ctx.mark_non_differentiable(ids, z, bary)
@@ -469,9 +476,9 @@ class _RasterSamples(torch.autograd.Function):
 
   @staticmethod
   def backward(ctx, d_out, d_vp, *unused):
-    attributes, clip, bary, triangles, ids, z = ctx.saved_tensors
+    attributes, clip, bary, triangles, ids, z, vp, vids = ctx.saved_tensors
     d_attr, d_clip, _ = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles,
-                                     ids, z, False)
+                                     ids, z, False, vp, vids)
     return (d_attr if ctx.needs_input_grad[0] else None,
             d_clip if ctx.needs_input_grad[1] else None, None, None, None, None)
 
@@ -480,7 +487,10 @@ def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, wor
   """Rasterizes a packed batch and, in the same pass, interpolates
   ``attributes`` [sum V, K <= 16] (background 0) and computes the splat
   positions. Returns (attributes [L*P, K], positions [L*P, 4], ids, z, bary);
-  the first two are differentiable w.r.t. ``attributes`` and ``clip``."""
+  the first two are differentiable w.r.t. ``attributes`` and ``clip``.
+  Positions are written for foreground samples only, as (viewport xyz,
+  clip w): splat them with ``z`` so that the depth buffer marks the
+  background."""
   _require_cuda(clip, triangles)
   attributes = _f32(attributes)
   if attributes.shape[1] > _lib.DR_MAX_CHANNELS:

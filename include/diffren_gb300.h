@@ -121,9 +121,12 @@ int dr_rasterize_batch(const float* vertices, const int32_t* triangles,
 
 /* dr_rasterize_batch fused with dr_interpolate_with_positions_fwd: the
  * rasterizer's epilogue, which already holds each layer sample's triangle
- * and barycentrics, also writes the splat position (viewport xyz, fg)
- * `positions` [L, H_i, W_i, 4] of every foreground sample (background
- * entries are left unwritten: pass z_buffer to the splat) and, when
+ * and barycentrics, also writes the splat position `positions`
+ * [L, H_i, W_i, 4] of every foreground sample as (viewport xyz, clip w)
+ * (background entries are left unwritten: pass z_buffer to the splat,
+ * which then takes the foreground from it), when `vertex_ids` is non-null
+ * the foreground samples' three vertex indices [L, H_i, W_i, 3] (the
+ * Framebuffer's vertex_ids, rasterize.py:111-113) and, when
  * `attributes` [V, K] is non-null,
  * the interpolated attributes `attributes_out` [L, H_i, W_i, K] (background
  * 0) (interpolate.py:24-63, splat.py:207-221). Same bits as the separate
@@ -134,7 +137,8 @@ int dr_rasterize_batch_interpolate(const float* vertices, const int32_t* triangl
                                    const dr_raster_config* config, int32_t* triangle_ids,
                                    float* z_buffer, float* barycentrics,
                                    const float* attributes, int32_t num_channels,
-                                   float* attributes_out, float* positions, void* workspace,
+                                   float* attributes_out, float* positions,
+                                   int32_t* vertex_ids, void* workspace,
                                    size_t workspace_bytes, void* stream);
 
 size_t dr_rasterize_triangles_workspace_bytes(int32_t num_triangles,
@@ -277,12 +281,16 @@ int dr_interpolate_with_positions_fwd(const float* attributes, int32_t num_chann
 
 /* Its VJP: from d_attributes_out (nullable) and d_positions, accumulates
  * d_attributes [V, K] and d_clip_vertices [V, 4] (caller zeroes both) and
- * writes d_barycentrics when non-null. */
+ * writes d_barycentrics when non-null. `positions` and `vertex_ids`
+ * (nullable) are dr_rasterize_batch_interpolate's: with them the VJP reads
+ * each foreground sample's vertex indices and clip w instead of gathering
+ * its triangle and clip vertices. */
 int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       const float* d_positions, const float* attributes,
                                       int32_t num_channels, const float* clip_vertices,
                                       const int32_t* triangles, const int32_t* triangle_ids,
                                       const float* z_buffer, const float* barycentrics,
+                                      const float* positions, const int32_t* vertex_ids,
                                       const dr_image_desc* images, int32_t num_images,
                                       int32_t num_layers, float* d_attributes,
                                       float* d_clip_vertices, float* d_barycentrics,

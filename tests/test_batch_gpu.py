@@ -2,10 +2,13 @@
 equals its own render_triangles call, the rasterizer's fused interpolation
 equals the separate kernels bit for bit, and a CUDA-graph replay of a
 forward+backward step equals the eager step."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
 
+from diffren_gb300 import _lib
 from diffren_gb300 import batch as batch_lib
 from diffren_gb300 import constants, kernels, render, workloads
 
@@ -78,10 +81,32 @@ def test_fused_raster_interpolation_matches_separate_kernels(K, depth_mode, devi
                                                         z2, r.batch, 3)
   for a, b in [(ids, ids2), (z, z2), (bary, bary2), (out, out2)]:
     assert torch.equal(a, b)
-  # The fused pass writes positions of foreground samples only.
+  # The fused pass writes positions of foreground samples only, with the
+  # interpolated clip w in place of the foreground flag.
   fg = z != 1.0
-  assert torch.equal(vp[fg], vp2[fg])
-  assert (vp2[~fg][:, 3] == 0).all()
+  assert torch.equal(vp[fg][:, :3], vp2[fg][:, :3])
+  assert (vp2[~fg][:, 3] == 0).all() and (vp2[fg][:, 3] == 1).all()
+  img = torch.as_tensor(np.repeat(np.arange(r.batch.n), 3 * np.array(
+      [w * h for w, h in sizes])), device=device)
+  toff = torch.as_tensor(r.batch.triangle_offsets[:-1], device=device)
+  voff = torch.as_tensor(r.batch.vertex_offsets[:-1], device=device)
+  tri = r.triangles.long()[toff[img] + ids.long()]  # local vertex indices
+  vfg = voff[img][fg]
+  w_ref = (clip[vfg[:, None] + tri[fg]][..., 3] * bary[fg]).sum(-1)
+  torch.testing.assert_close(vp[fg][:, 3], w_ref, rtol=1e-6, atol=1e-6)
+  # The vertex indices it stores for the VJP are the triangles' rows.
+  vids = torch.full((ids.shape[0], 3), -7, dtype=torch.int32, device=device)
+  bufs = [torch.empty_like(t) for t in (ids, z, bary, out, vp)]
+  ws = kernels.Workspace(device).get(kernels.raster_workspace_bytes(r.batch, r.config))
+  p = kernels._p
+  rc = _lib.load().dr_rasterize_batch_interpolate(
+      p(clip), p(r.triangles), r.batch.ptr, r.batch.n, ctypes.byref(r.config), p(bufs[0]),
+      p(bufs[1]), p(bufs[2]), p(attr), K, p(bufs[3]), p(bufs[4]), p(vids), p(ws), ws.numel(),
+      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+  assert rc == 0
+  torch.cuda.synchronize()
+  assert torch.equal(vids[fg].long(), tri[fg])
+  assert (vids[~fg] == -7).all()
 
 
 def test_graph_replay_matches_eager(device):
