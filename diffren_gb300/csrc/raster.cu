@@ -9,6 +9,7 @@
 // pixel keeps the L smallest packed (depth | triangle id) keys, which is
 // independent of the order fragments arrive in.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <string>
 
@@ -28,8 +29,20 @@ struct __align__(16) TriSetup {
   long long m[9];  // edge-function coefficients (unnormalized inverse)
   float vz[3];     // clip z of the three vertices
   float vw[3];     // clip w of the three vertices
+  // The rest serves the fused epilogue only (the fine loop stages the first
+  // 96 bytes): vertex indices and clip x, y, so that a sample's
+  // interpolation reads one record instead of gathering its triangle and
+  // vertices.
+  int32_t vid[3];
+  float vx[3];
+  float vy[3];
+  int32_t pad[3];
 };
-static_assert(sizeof(TriSetup) == 96, "TriSetup layout");
+static_assert(sizeof(TriSetup) == 144, "TriSetup layout");
+static_assert(offsetof(TriSetup, vz) == 72 && offsetof(TriSetup, vw) == 84 &&
+                  offsetof(TriSetup, vid) == 96 && offsetof(TriSetup, vx) == 108 &&
+                  offsetof(TriSetup, vy) == 120,
+              "write_sample reads the record by these offsets");
 
 struct RasterArgs {
   const float4* verts;
@@ -131,10 +144,14 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
       if (valid) {
         s.vz[0] = v0.z; s.vz[1] = v1.z; s.vz[2] = v2.z;
         s.vw[0] = v0.w; s.vw[1] = v1.w; s.vw[2] = v2.w;
+        s.vid[0] = i0; s.vid[1] = i1; s.vid[2] = i2;
+        s.vx[0] = v0.x; s.vx[1] = v1.x; s.vx[2] = v2.x;
+        s.vy[0] = v0.y; s.vy[1] = v1.y; s.vy[2] = v2.y;
+        s.pad[0] = s.pad[1] = s.pad[2] = 0;
         const int4* src = reinterpret_cast<const int4*>(&s);
         int4* dst = reinterpret_cast<int4*>(a.setup + g);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) dst[k] = src[k];
+        for (int k = 0; k < 9; ++k) dst[k] = src[k];
       }
     }
   }
@@ -239,8 +256,9 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 // requested (the Framebuffer's vertex_ids, rasterize.py:111-113), and the
 // attributes (interpolate.py:24-63, background 0). The same operations, in
 // the same order, as samples_fwd_kernel on the stored buffers.
-__device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B, int img, int id,
-                                          float zz, const float b[3], int64_t o) {
+__device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B, int img,
+                                          const TriSetup* t, float zz, const float b[3],
+                                          int64_t o) {
   const SampleOutputs& so = a.so;
   const int K = so.K;
   const bool vec_rows = (K & 3) == 0;
@@ -248,10 +266,20 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
   float* ao = so.attr ? so.attr_out + o * K : nullptr;
   const bool fg = zz != 1.0f;
   if (fg) {
-    const int32_t* t = a.tris + 3 * (B.triangle_offset[img] + id);
-    const int v0 = __ldg(t), v1 = __ldg(t + 1), v2 = __ldg(t + 2);
-    const float4* vb = a.verts + B.vertex_offset[img];
-    c = lerp_clip(__ldg(vb + v0), __ldg(vb + v1), __ldg(vb + v2), b);
+    // One record holds the vertex indices and clip coordinates (the sample
+    // is foreground, so its key and record exist).
+    const float2 z01 = __ldg(reinterpret_cast<const float2*>(t->vz));
+    const int4 r5 = __ldg(reinterpret_cast<const int4*>(t) + 5);  // vz2, vw0..2
+    const int4 r6 = __ldg(reinterpret_cast<const int4*>(t) + 6);  // vid0..2, vx0
+    const int4 r7 = __ldg(reinterpret_cast<const int4*>(t) + 7);  // vx1, vx2, vy0, vy1
+    const int4 r8 = __ldg(reinterpret_cast<const int4*>(t) + 8);  // vy2
+    const int v0 = r6.x, v1 = r6.y, v2 = r6.z;
+    c = lerp_clip(make_float4(__int_as_float(r6.w), __int_as_float(r7.z), z01.x,
+                              __int_as_float(r5.y)),
+                  make_float4(__int_as_float(r7.x), __int_as_float(r7.w), z01.y,
+                              __int_as_float(r5.z)),
+                  make_float4(__int_as_float(r7.y), __int_as_float(r8.x),
+                              __int_as_float(r5.x), __int_as_float(r5.w)), b);
     if (ao) {
       const float* ab = so.attr + B.vertex_offset[img] * K;
       const float* a0 = ab + int64_t(v0) * K;
@@ -450,12 +478,13 @@ __global__ void __launch_bounds__(kThreads, kFused ? 4 : 5) fine_raster_kernel(R
         float b[3] = {0.0f, 0.0f, 0.0f};
         int id;
         float zz;
+        const TriSetup* st = nullptr;
         if (key == kEmpty) {
           id = disc ? 0 : -1;
           zz = 1.0f;
         } else {
           id = int(uint32_t(key));
-          const TriSetup* st = a.setup + tri0 + id;
+          st = a.setup + tri0 + id;
           long long m[9];
 #pragma unroll
           for (int q = 0; q < 9; ++q) m[q] = __ldg(&st->m[q]);
@@ -478,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, kFused ? 4 : 5) fine_raster_kernel(R
         bo[0] = b[0];
         bo[1] = b[1];
         bo[2] = b[2];
-        if (kFused) write_sample(a, B, img, id, zz, b, o);
+        if (kFused) write_sample(a, B, img, st, zz, b, o);
       }
     }
     __syncthreads();

@@ -251,6 +251,14 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
   int64_t e[kVjpPerThread];
   bool fg[kVjpPerThread];
   int nfg = 0;
+  // The thread's samples are consecutive: find the first one's image, then
+  // step to the next image only where a sample crosses into it.
+  int cur = 0;
+  int64_t cur_end = 0, local0 = 0;
+  if (q0 < total) {
+    cur = locate(B, p.L, q0, local0);
+    cur_end = int64_t(p.L) * B.pix_prefix[cur + 1];
+  }
 #pragma unroll
   for (int u = 0; u < kVjpPerThread; ++u) {
     const int64_t q = q0 + u;
@@ -258,9 +266,12 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
     e[u] = 0;
     fg[u] = false;
     if (q < total) {
-      int64_t local;
-      img[u] = locate(B, p.L, q, local);
-      e[u] = int64_t(p.L) * B.pix_off[img[u]] + local;
+      while (q >= cur_end) {
+        ++cur;
+        cur_end = int64_t(p.L) * B.pix_prefix[cur + 1];
+      }
+      img[u] = cur;
+      e[u] = int64_t(p.L) * B.pix_off[cur] + (q - int64_t(p.L) * B.pix_prefix[cur]);
     }
   }
 #pragma unroll
