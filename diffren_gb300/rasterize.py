@@ -100,13 +100,18 @@ def rasterize_geometry(geom: Geometry, num_layers, face_culling_mode,
   if compute_diff_barys:
     bary = kernels.diff_barycentrics_packed(geom.clip, geom.triangles_packed, ids, z,
                                             geom.batch, num_layers)
+  return framebuffer_of(geom, num_layers, ids, z, bary), (ids, z, bary)
+
+
+def framebuffer_of(geom: Geometry, num_layers, ids, z, bary):
+  """Framebuffer views of flat rasterizer outputs."""
   H, W = geom.batch.heights[0], geom.batch.widths[0]
   shape = (geom.B, num_layers, H, W) if geom.batched else (num_layers, H, W)
   frame = fb.Framebuffer(barycentrics=bary.view(*shape, 3),
                          triangle_id=ids.view(*shape, 1), z_buffer=z.view(*shape),
                          triangles=geom.triangles)
   frame.packed = (geom.batch, geom.triangles_packed, ids, z)
-  return frame, (ids, z, bary)
+  return frame
 
 
 def rasterize_triangles(vertices, triangles, camera: Optional[torch.Tensor],

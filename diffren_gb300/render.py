@@ -18,6 +18,7 @@ import torch
 from . import composite
 from . import constants
 from . import interpolate
+from . import kernels
 from . import rasterize
 from . import splat
 
@@ -35,6 +36,35 @@ def _shade_layers(shading_function, interpolated, num_layers, batched):
   return torch.stack([
       shading_function({k: v[l] for k, v in interpolated.items()})
       for l in range(num_layers)])
+
+
+def _render_fused(geom, attributes, shading_function, num_layers, face_culling_mode,
+                  depth_semantics, return_accum_buffers):
+  """SPLAT_OVER through the rasterizer that interpolates the attributes and
+  the splat positions in its epilogue; None when the attributes exceed its
+  channel limit."""
+  keys = list(attributes.keys())
+  parts = []
+  for k in keys:
+    a = torch.as_tensor(attributes[k], device=geom.clip.device)
+    a = a.float() if not a.is_floating_point() or a.dtype != torch.float32 else a
+    if geom.batched:
+      a = (a.expand(geom.B, *a.shape) if a.dim() == 2 else a).reshape(-1, a.shape[-1])
+    parts.append(a)
+  widths = [p.shape[1] for p in parts]
+  if sum(widths) > kernels._lib.DR_MAX_CHANNELS:
+    return None
+  cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0].contiguous()
+  cfg = kernels.raster_config(num_layers, face_culling_mode, int(depth_semantics))
+  interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
+      cat, geom.clip, geom.triangles_packed, geom.batch, cfg,
+      kernels.default_workspace(geom.clip.device))
+  frame = rasterize.framebuffer_of(geom, num_layers, ids, z, bary)
+  lead = (geom.B,) if geom.batched else ()
+  interp = interp.view(*lead, num_layers, frame.height, frame.width, -1)
+  interpolated = dict(zip(keys, torch.split(interp, widths, dim=-1)))
+  shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
+  return splat.splat_positions(vp, frame, shaded, return_accum_buffers)
 
 
 def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
@@ -64,6 +94,12 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   rasterize._validate(vertices, triangles, camera, image_width, image_height,
                       num_layers)
   geom = rasterize.Geometry(vertices, triangles, camera, image_width, image_height)
+  if (compositing_mode == constants.CompositingMode.SPLAT_OVER and not compute_diff_barys
+      and attributes):
+    fused = _render_fused(geom, attributes, shading_function, num_layers,
+                          face_culling_mode, depth_semantics, return_accum_buffers)
+    if fused is not None:
+      return fused
   frame, _ = rasterize.rasterize_geometry(geom, num_layers, face_culling_mode,
                                           depth_semantics, compute_diff_barys)
   interpolated = interpolate.interpolate_vertex_attributes(attributes, frame)

@@ -53,9 +53,18 @@ def splat_at_pixel_centers(xyz_layers, color_layers, foreground_mask):
 def splat_clip(clip, frame: fb.Framebuffer, shaded_pixels, return_accum_buffers=False):
   """Splat with precomputed clip-space vertices (packed like the framebuffer)."""
   batch, tris, ids, z, bary = frame.kernel_inputs()
-  colors = _shaded_flat(shaded_pixels)
   vp = kernels.splat_positions_packed(clip, bary, tris, ids, z, batch, frame.num_layers)
-  res = kernels.splat_packed(vp, colors, batch, frame.num_layers, return_accum_buffers, z=z)
+  return splat_positions(vp, frame, shaded_pixels, return_accum_buffers)
+
+
+def splat_positions(positions, frame: fb.Framebuffer, shaded_pixels,
+                    return_accum_buffers=False):
+  """Splat at packed splat positions [L*P, 4] of the framebuffer's samples
+  (background samples are taken from its depth buffer)."""
+  batch, _, _, z, _ = frame.kernel_inputs()
+  colors = _shaded_flat(shaded_pixels)
+  res = kernels.splat_packed(positions, colors, batch, frame.num_layers,
+                             return_accum_buffers, z=z)
   lead = (frame.batch_size,) if frame.is_batched else ()
   return _shape_outputs(res, lead, frame.height, frame.width, colors.shape[1],
                         return_accum_buffers)

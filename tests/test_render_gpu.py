@@ -215,3 +215,22 @@ def test_render_matches_oracle_pipeline(device):
   shaded = np.concatenate([rgb, np.ones_like(rgb[..., :1])], -1)
   ref, _, _ = np_splat.splat_shaded_pixels(clip, ids, z, b, m.triangles, shaded, 128, 128)
   np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+
+
+def test_render_wide_attributes_fall_back_to_separate_kernels(device):
+  """More than 16 attribute channels skip the fused rasterizer; the image is
+  the same bits as the fused path's."""
+  m = workloads.icosphere_workload(6, seed=4)
+  cam = torch.tensor(workloads.camera_matrix((0.3, 0.2, 2.5), 48, 40), device=device)
+  v = torch.tensor(m.vertices, device=device)
+  t = torch.tensor(m.triangles, device=device)
+  rgb = torch.tensor(m.colors, device=device)
+  extra = torch.rand(len(m.vertices), 14, device=device)
+
+  def shade(a):
+    return torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1)
+
+  fused = render.render_triangles(v, {"rgb": rgb}, t, cam, 48, 40, shade, num_layers=3)
+  wide = render.render_triangles(v, {"rgb": rgb, "extra": extra}, t, cam, 48, 40, shade,
+                                 num_layers=3)
+  assert torch.equal(fused, wide)
