@@ -14,7 +14,8 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 
 def declarations():
-  src = open(HEADER).read()
+  with open(HEADER) as f:
+    src = f.read()
   src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
   decls = {}
   for m in re.finditer(r"\b(dr_\w+)\s*\(([^)]*)\)\s*;", src):
@@ -105,7 +106,8 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
 
 
 def test_python_constants_match_header():
-  src = open(HEADER).read()
+  with open(HEADER) as f:
+    src = f.read()
   for name in ("DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_MAX_IMAGE_DIM",
                "DR_MAX_SPLAT_CHANNELS", "DR_OK",
                "DR_CULL_NONE", "DR_CULL_BACK", "DR_CULL_FRONT", "DR_DEPTH_DISCRETIZED",

@@ -29,7 +29,7 @@ def _rank(rank, world, port, times, out):
 def test_max_over_ranks_with_two_gloo_ranks():
   world, port = 2, _free_port()
   times = [3.5, 7.25]
-  with mp.Manager() as manager:
+  with mp.get_context("spawn").Manager() as manager:
     out = manager.dict()
     mp.start_processes(_rank, args=(world, port, times, out), nprocs=world,
                        start_method="spawn")
