@@ -21,7 +21,10 @@ static_assert(dr::kErrorFlagsOffset == 4, "error word is counters[1]");
 namespace dr {
 namespace {
 
-constexpr int kThreads = 256;  // fine-raster block = triangle chunk size
+// Fine-raster block = triangle chunk size. 128-thread blocks keep eight
+// tiles in flight per SM (each tile's setup, scan and epilogue are serial
+// latency chains), which measured faster than four 256-thread tiles.
+constexpr int kThreads = 128;
 constexpr int kDefaultTile = 16;
 constexpr int kDefaultLargeTiles = 16;
 
@@ -313,11 +316,10 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
   }
 }
 
-// kFused adds the sample outputs to the epilogue; it needs more registers,
-// so it is a separate instantiation with its own occupancy. LT > 0 fixes the
-// layer count at compile time (the common L = 3), LT = 0 reads it.
+// kFused adds the sample outputs to the epilogue. LT > 0 fixes the layer
+// count at compile time (the common L = 3), LT = 0 reads it.
 template <bool kFused, int LT>
-__global__ void __launch_bounds__(kThreads, kFused ? 4 : 5) fine_raster_kernel(RasterArgs a,
+__global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
                                                                              Batch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_warp[kThreads / 32];
