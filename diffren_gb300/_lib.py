@@ -18,6 +18,8 @@ DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
 DR_MAX_BATCH_INLINE = 128
+DR_TEXTURE_PAD_ZERO = 1
+DR_TEXTURE_TEXEL_UNITS = 2
 DR_MAX_IMAGE_DIM = 32768
 DR_STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -25,6 +27,7 @@ DR_STATIC_SCRATCH_BYTES = 64 << 20
 _P = ctypes.c_void_p
 _I = ctypes.c_int32
 _S = ctypes.c_size_t
+_L = ctypes.c_int64
 
 
 class ImageDesc(ctypes.Structure):
@@ -69,6 +72,8 @@ SIGNATURES = {
                                               _P, _I, _I, _P, _P, _P, _P]),
     "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
+    "dr_texture_map_fwd": (_I, [_P, _L, _P, _I, _I, _I, _I, _P, _P]),
+    "dr_texture_map_bwd": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
     "dr_splat_bwd": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),
 }

@@ -239,6 +239,26 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                 err);
 }
 
+int dr_texture_map_fwd(const float* uv, int64_t num_points, const float* texture,
+                       int32_t height, int32_t width, int32_t channels, int32_t flags,
+                       float* out, void* stream) {
+  std::string err;
+  return finish(dr::texture_fwd_launch(uv, num_points, texture, height, width, channels,
+                                       flags, out, as_stream(stream), err),
+                err);
+}
+
+int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
+                       const float* texture, int32_t height, int32_t width,
+                       int32_t channels, int32_t flags, float* d_uv, float* d_texture,
+                       void* stream) {
+  std::string err;
+  return finish(dr::texture_bwd_launch(d_out, uv, num_points, texture, height, width,
+                                       channels, flags, d_uv, d_texture, as_stream(stream),
+                                       err),
+                err);
+}
+
 int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
                            const int32_t* triangle_ids, const float* z_buffer,
                            const float* barycentrics, const dr_image_desc* images,

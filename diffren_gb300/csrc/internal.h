@@ -101,6 +101,13 @@ int diffbary_bwd_launch(const float* d_bary, const float* clip, const int32_t* t
                         const dr_image_desc* images, int n, int L, float* d_clip,
                         cudaStream_t stream, std::string& err);
 
+// texture.cu
+int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int W, int C,
+                       int flags, float* out, cudaStream_t stream, std::string& err);
+int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const float* tex,
+                       int H, int W, int C, int flags, float* d_uv, float* d_tex,
+                       cudaStream_t stream, std::string& err);
+
 // splat.cu
 int samples_fwd_launch(const float* attributes, int K, const float* clip,
                        const int32_t* tris, const int32_t* ids, const float* z,

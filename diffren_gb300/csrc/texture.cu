@@ -1,0 +1,174 @@
+// Texture-map shader (diffren/jax/utils/shaders.py:40-65) and its VJP:
+// bilinear resampling of an [H, W, C] texture at uv * (W, H) with the
+// texture padded by one edge texel (image.py:21-118, pad_mode='edge'), or by
+// zeros (pad_mode='constant') and at locations in texel units, as
+// image.bilinear_resample.
+//
+// Per point: location (row, col) = (v H, u W) - 0.5 + 1 in padded texels,
+// floor clipped to [0, size], ceil weight clip(location - floor, 0, 1),
+// result ((ll + ul) + ur) + lr with each corner (texel * w_row) * w_col: the
+// reference's expression order, so results are the reference's bits. The
+// VJP scatters to the four texels (float atomics) and differentiates the
+// weights, with jnp.clip's gradient (1 strictly inside its bounds).
+#include <algorithm>
+#include <string>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace dr {
+namespace {
+
+struct TexArgs {
+  const float* uv;
+  const float* tex;
+  int H, W, C, flags;
+  int64_t n;
+  float* out;
+  const float* d_out;
+  float* d_uv;
+  float* d_tex;
+};
+
+struct Axis {
+  int f;      // floor index in padded texels, in [0, size]
+  float cw;   // ceil weight
+  float fw;   // floor weight
+  float dcw;  // d cw / d location (1 strictly inside (0, 1), else 0)
+};
+
+__device__ __forceinline__ Axis axis_of(float loc, int size) {
+  Axis a;
+  const float fl = fminf(fmaxf(floorf(loc), 0.0f), __int2float_rn(size));
+  a.f = __float2int_rz(fl);
+  const float t = __fsub_rn(loc, fl);
+  a.cw = fminf(fmaxf(t, 0.0f), 1.0f);
+  a.fw = __fsub_rn(1.0f, a.cw);
+  a.dcw = (t > 0.0f && t < 1.0f) ? 1.0f : 0.0f;
+  return a;
+}
+
+// Texel (r, c) of the padded texture: padded index minus one, clamped to
+// the edge; -1 for the zero border of constant padding.
+__device__ __forceinline__ int64_t texel(const TexArgs& a, int r, int c) {
+  if ((a.flags & DR_TEXTURE_PAD_ZERO) && (r == 0 || c == 0 || r > a.H || c > a.W)) return -1;
+  r = min(max(r - 1, 0), a.H - 1);
+  c = min(max(c - 1, 0), a.W - 1);
+  return (int64_t(r) * a.W + c) * a.C;
+}
+
+__device__ __forceinline__ float fetch(const TexArgs& a, int64_t t, int k) {
+  return t < 0 ? 0.0f : __ldg(a.tex + t + k);
+}
+
+struct Footprint {
+  Axis r, c;
+  int64_t t00, t10, t11, t01;
+};
+
+__device__ __forceinline__ Footprint footprint(const TexArgs& a, int64_t i) {
+  Footprint f;
+  const float u = __ldg(a.uv + 2 * i), v = __ldg(a.uv + 2 * i + 1);
+  // query = uv * (W, H) - 0.5 (or texel units - 0.5), then + 1 into the
+  // padded texture
+  const bool texels = a.flags & DR_TEXTURE_TEXEL_UNITS;
+  const float qc = __fsub_rn(texels ? u : __fmul_rn(u, __int2float_rn(a.W)), 0.5f);
+  const float qr = __fsub_rn(texels ? v : __fmul_rn(v, __int2float_rn(a.H)), 0.5f);
+  f.r = axis_of(__fadd_rn(qr, 1.0f), a.H);
+  f.c = axis_of(__fadd_rn(qc, 1.0f), a.W);
+  f.t00 = texel(a, f.r.f, f.c.f);
+  f.t10 = texel(a, f.r.f + 1, f.c.f);
+  f.t11 = texel(a, f.r.f + 1, f.c.f + 1);
+  f.t01 = texel(a, f.r.f, f.c.f + 1);
+  return f;
+}
+
+__global__ void __launch_bounds__(256) texture_fwd_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const Footprint f = footprint(a, i);
+  float* o = a.out + i * a.C;
+  for (int k = 0; k < a.C; ++k) {
+    const float ll = __fmul_rn(__fmul_rn(fetch(a, f.t00, k), f.r.fw), f.c.fw);
+    const float ul = __fmul_rn(__fmul_rn(fetch(a, f.t10, k), f.r.cw), f.c.fw);
+    const float ur = __fmul_rn(__fmul_rn(fetch(a, f.t11, k), f.r.cw), f.c.cw);
+    const float lr = __fmul_rn(__fmul_rn(fetch(a, f.t01, k), f.r.fw), f.c.cw);
+    o[k] = __fadd_rn(__fadd_rn(__fadd_rn(ll, ul), ur), lr);
+  }
+}
+
+__global__ void __launch_bounds__(256) texture_bwd_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const float* g = a.d_out + i * a.C;
+  bool any = false;
+  for (int k = 0; k < a.C; ++k) any |= __ldg(g + k) != 0.0f;
+  if (!any) {
+    if (a.d_uv) {
+      a.d_uv[2 * i] = 0.0f;
+      a.d_uv[2 * i + 1] = 0.0f;
+    }
+    return;
+  }
+  const Footprint f = footprint(a, i);
+  float du = 0.0f, dv = 0.0f;
+  for (int k = 0; k < a.C; ++k) {
+    const float gk = __ldg(g + k);
+    if (a.d_tex && gk != 0.0f) {
+      if (f.t00 >= 0) atomicAdd(a.d_tex + f.t00 + k, gk * f.r.fw * f.c.fw);
+      if (f.t10 >= 0) atomicAdd(a.d_tex + f.t10 + k, gk * f.r.cw * f.c.fw);
+      if (f.t11 >= 0) atomicAdd(a.d_tex + f.t11 + k, gk * f.r.cw * f.c.cw);
+      if (f.t01 >= 0) atomicAdd(a.d_tex + f.t01 + k, gk * f.r.fw * f.c.cw);
+    }
+    if (a.d_uv) {
+      const float d00 = fetch(a, f.t00, k), d10 = fetch(a, f.t10, k);
+      const float d11 = fetch(a, f.t11, k), d01 = fetch(a, f.t01, k);
+      du += gk * (f.r.fw * (d01 - d00) + f.r.cw * (d11 - d10));
+      dv += gk * (f.c.fw * (d10 - d00) + f.c.cw * (d11 - d01));
+    }
+  }
+  if (a.d_uv) {
+    const bool texels = a.flags & DR_TEXTURE_TEXEL_UNITS;
+    a.d_uv[2 * i] = du * f.c.dcw * (texels ? 1.0f : __int2float_rn(a.W));
+    a.d_uv[2 * i + 1] = dv * f.r.dcw * (texels ? 1.0f : __int2float_rn(a.H));
+  }
+}
+
+bool check_tex(const float* uv, int64_t n, const float* tex, int H, int W, int C,
+               std::string& err) {
+  if (n < 0 || H < 1 || W < 1 || C < 1 || C > DR_MAX_CHANNELS || H >= (1 << 28) ||
+      W >= (1 << 28)) {
+    err = "texture must be [H >= 1, W >= 1, 1 <= C <= 16] and the point count >= 0";
+    return false;
+  }
+  if (n > 0 && (!uv || !tex)) {
+    err = "uv and texture must be non-null";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int W, int C,
+                       int flags, float* out, cudaStream_t stream, std::string& err) {
+  if (!check_tex(uv, n, tex, H, W, C, err)) return DR_ERR_INVALID_ARGUMENT;
+  if (n == 0) return DR_OK;
+  if (!out) { err = "out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
+  TexArgs a{uv, tex, H, W, C, flags, n, out, nullptr, nullptr, nullptr};
+  texture_fwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  return launch_status("texture map", err);
+}
+
+int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const float* tex,
+                       int H, int W, int C, int flags, float* d_uv, float* d_tex,
+                       cudaStream_t stream, std::string& err) {
+  if (!check_tex(uv, n, tex, H, W, C, err)) return DR_ERR_INVALID_ARGUMENT;
+  if (n == 0) return DR_OK;
+  if (!d_out) { err = "d_out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
+  TexArgs a{uv, tex, H, W, C, flags, n, nullptr, d_out, d_uv, d_tex};
+  texture_bwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  return launch_status("texture map backward", err);
+}
+
+}  // namespace dr

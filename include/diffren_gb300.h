@@ -38,6 +38,8 @@
  *       (diffren/jax/internal/rasterize.py:127-255) and its VJP.
  *   dr_splat_positions_fwd/bwd -> the clip-space interpolation and viewport
  *       transform of splat.splat_shaded_pixels (splat.py:207-221) and its VJP.
+ *   dr_texture_map_fwd/bwd  -> utils.shaders.texture_map
+ *       (diffren/jax/utils/shaders.py:40-65, utils/image.py:21-118).
  *   dr_splat_fwd/bwd        -> splat.splat_at_pixel_centers + composite.over
  *       (diffren/jax/internal/splat.py:26-175, diffren/jax/composite.py:20-37)
  *       and their VJP.
@@ -295,6 +297,28 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       int32_t num_layers, float* d_attributes,
                                       float* d_clip_vertices, float* d_barycentrics,
                                       void* stream);
+
+/* ---------------------------------------------------------- shaders */
+
+/* shaders.texture_map (diffren/jax/utils/shaders.py:40-65): bilinear
+ * resampling (image.py:21-118) of a float [height, width, channels] texture
+ * at uv [num_points, 2] (u along the width), out [num_points, channels],
+ * with the reference's expression order. flags: DR_TEXTURE_PAD_ZERO pads
+ * with zeros instead of the edge texels (pad_mode='constant'),
+ * DR_TEXTURE_TEXEL_UNITS takes the points in texel units instead of uv
+ * (image.bilinear_resample's locations). */
+#define DR_TEXTURE_PAD_ZERO 1
+#define DR_TEXTURE_TEXEL_UNITS 2
+int dr_texture_map_fwd(const float* uv, int64_t num_points, const float* texture,
+                       int32_t height, int32_t width, int32_t channels, int32_t flags,
+                       float* out, void* stream);
+
+/* Its VJP: d_uv [num_points, 2] is written (nullable), d_texture
+ * [height, width, channels] accumulated (nullable; caller zeroes it). */
+int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
+                       const float* texture, int32_t height, int32_t width,
+                       int32_t channels, int32_t flags, float* d_uv, float* d_texture,
+                       void* stream);
 
 /* splat_at_pixel_centers + composite.over (splat.py:26-175,
  * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the

@@ -12,6 +12,7 @@ decodes the small golden PNGs the GPU tests compare against. Nothing here is
 used at run time by the library.
 """
 import argparse
+import ast
 import os
 import re
 import sys
@@ -64,6 +65,66 @@ def jacobian_known_answer(path):
   src = open(path).read()
   m = re.search(r"expected_jacobian = np\.array\((\[.*?\])\)", src, re.S)
   return np.array(_floats(m.group(1)), np.float32).reshape(3, 3, 3)
+
+
+def textured_square_inputs(path):
+  """Clip coordinates, uvs and 2x2 texture of shaders_test.py's textured
+  square (its 4:3 scaling of x included)."""
+  src = open(path).read()
+  body = src[src.index("def test_textured_square"):]
+  body = body[:body.index("rendered = ")]
+  arrays = re.findall(r"jnp\.array\(\s*(\[.*?\])\s*(?:,\s*dtype=[^)]*)?\)", body, re.S)
+  clip = np.array(_floats(arrays[0]), np.float32).reshape(4, 4)
+  uv = np.array(_floats(arrays[1]), np.float32).reshape(4, 2)
+  tex = np.array(_floats(arrays[2]), np.float32).reshape(2, 2, 3)
+  m = re.search(r"clip_coordinates\.at\[:, 0\]\.multiply\(([0-9.]+)\)", body)
+  clip[:, 0] *= np.float32(float(m.group(1)))
+  tris = re.search(r"\{'uv': uv_coordinates\},\s*(\(\(.*?\)\)),", src, re.S)
+  tri = np.array(_floats(tris.group(1)), np.int32).reshape(-1, 3)
+  return {"textured_square_clip": clip, "textured_square_uv": uv,
+          "textured_square_texture": tex, "textured_square_triangles": tri}
+
+
+def _safe_number(text, names):
+  """Value of a small arithmetic expression of the test source: numbers, the
+  given names, + - * /, unary minus, parentheses and float('inf')."""
+  def ev(node):
+    if isinstance(node, ast.Expression):
+      return ev(node.body)
+    if isinstance(node, ast.Constant) and isinstance(node.value, (int, float)):
+      return float(node.value)
+    if isinstance(node, ast.Name) and node.id in names:
+      return float(names[node.id])
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, (ast.USub, ast.UAdd)):
+      v = ev(node.operand)
+      return -v if isinstance(node.op, ast.USub) else v
+    if isinstance(node, ast.BinOp) and isinstance(node.op, (ast.Add, ast.Sub, ast.Mult,
+                                                            ast.Div)):
+      a, b = ev(node.left), ev(node.right)
+      return {ast.Add: a + b, ast.Sub: a - b, ast.Mult: a * b,
+              ast.Div: a / b if b else float("nan")}[type(node.op)]
+    if (isinstance(node, ast.Call) and isinstance(node.func, ast.Name) and
+        node.func.id == "float" and len(node.args) == 1 and
+        isinstance(node.args[0], ast.Constant) and node.args[0].value in ("inf", "-inf")):
+      return float(node.args[0].value)
+    raise ValueError("unexpected expression in test data: %r" % text)
+  return ev(ast.parse(text.strip(), mode="eval"))
+
+
+def bilinear_boundary_cases(path):
+  """(x, y) samples and expected values of image_test.py's boundary test
+  on its 30 x 10 ramp image (values 1..10 along x)."""
+  src = open(path).read()
+  body = src[src.index("test_case_list = [") + len("test_case_list = ["):]
+  body = body[:body.index("# pyformat: enable")]
+  rows = re.findall(r"\[\[\s*([^\[\]]+?)\s*\],\s*([^\[\]]+?)\]", body)
+  names = {"image_width": 10, "image_height": 30}
+  samples, expected = [], []
+  for pt, val in rows:
+    samples.append([_safe_number(t, names) for t in pt.split(",")])
+    expected.append(_safe_number(val, names))
+  return {"samples": np.array(samples, np.float32), "expected": np.array(expected, np.float32),
+          "shape": np.array([30, 10], np.int32)}
 
 
 def main():
@@ -137,8 +198,16 @@ def main():
       imgs["unlit_cube_%d_%d" % (i, l)] = png.read_png(
           os.path.join(data, "Unlit_Cube_%d_%d.png" % (i, l)))
   imgs["spike_derivative"] = png.read_png(os.path.join(data, "Spike_Derivative.png"))
+  imgs["textured_square"] = png.read_png(os.path.join(data, "Textured_Square.png"))
+  imgs.update(textured_square_inputs(os.path.join(ref, "diffren", "jax", "utils",
+                                                   "shaders_test.py")))
   imgs["sphere_disparity"] = png.read_png(os.path.join(data, "Sphere_Disparity.png"))
   np.savez_compressed(os.path.join(HERE, "render_goldens.npz"), **imgs)
+
+  # Bilinear resampling known answers (image_test.py boundary cases).
+  np.savez_compressed(os.path.join(HERE, "texture_cases.npz"),
+                      **bilinear_boundary_cases(os.path.join(ref, "diffren", "jax", "utils",
+                                                             "image_test.py")))
   for f in sorted(os.listdir(HERE)):
     if f.endswith(".npz"):
       print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -228,3 +228,40 @@ def test_torch_oracle_gradient_matches_finite_differences():
     cm[vi, k] -= eps
     fd = (loss(cp, s) - loss(cm, s)).item() / (2 * eps)
     assert abs(fd - gc[vi, k].item()) <= 1e-4 * max(1.0, abs(fd)) + 1e-5, (vi, k, fd, gc[vi, k])
+
+
+# ------------------------------------------------------------ texture map
+def test_texture_oracle_recovers_input_at_texel_centers():
+  """image_test.py:26-41: sampling at (x, y) + 0.5 returns the image."""
+  from oracle import texture
+  n = 64
+  img = np.arange(3 * n * n).reshape(n, n, 3).astype(np.float32)
+  x, y = np.meshgrid(np.arange(n), np.arange(n))
+  out = texture.bilinear_resample(img, np.stack((x, y), -1) + 0.5)
+  np.testing.assert_array_equal(out, img)
+
+
+def test_texture_oracle_boundary_cases():
+  """image_test.py:44-119: the reference's boundary samples (zero padding)
+  on its 30 x 10 ramp image."""
+  from oracle import texture
+  g = np.load(os.path.join(os.path.dirname(__file__), "golden", "texture_cases.npz"))
+  h, w = g["shape"]
+  img = np.repeat(np.arange(1, w + 1, dtype=np.float32)[None], h, 0)[..., None].repeat(3, 2)
+  out = texture.bilinear_resample(img, g["samples"])
+  np.testing.assert_array_almost_equal(out, g["expected"][:, None].repeat(3, 1), decimal=5)
+
+
+def test_texture_oracle_torch_matches_numpy_and_finite_differences():
+  import torch
+  from oracle import texture
+  rng = np.random.default_rng(3)
+  tex = rng.uniform(0, 1, (5, 7, 2)).astype(np.float32)
+  uv = rng.uniform(-0.2, 1.2, (400, 2)).astype(np.float32)
+  a = texture.texture_map(uv, tex)
+  b = texture.texture_map_t(torch.tensor(uv), torch.tensor(tex)).numpy()
+  np.testing.assert_array_equal(a, b)
+  t = torch.tensor(tex, dtype=torch.float64, requires_grad=True)
+  u = torch.tensor(uv, dtype=torch.float64, requires_grad=True)
+  assert torch.autograd.gradcheck(lambda uu, tt: texture.texture_map_t(uu, tt), (u, t),
+                                  eps=1e-6, atol=1e-5)

@@ -1,0 +1,89 @@
+"""Texture-map shader kernel (shaders.py:40-65, image.py:21-118) against the
+CPU restatement, the reference's own resampling known answers and its
+textured-square golden render."""
+import numpy as np
+import pytest
+import torch
+
+import helpers
+from diffren_gb300 import render, shaders
+from oracle import texture
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-4
+
+
+def assert_grad_close(ours, ref):
+  ours, ref = np.asarray(ours, np.float64), np.asarray(ref, np.float64)
+  scale = float(np.abs(ref).max()) or 1.0
+  np.testing.assert_allclose(ours, ref, rtol=GRAD_RTOL, atol=GRAD_RTOL * scale)
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 3), (16, 9, 4), (1, 1, 1), (33, 2, 2), (8, 8, 16)])
+def test_texture_map_forward_matches_oracle(shape, device):
+  rng = np.random.default_rng(sum(shape))
+  tex = rng.uniform(-1, 1, shape).astype(np.float32)
+  uv = rng.uniform(-0.3, 1.3, (3000, 2)).astype(np.float32)
+  # texel centers, edges and corners exactly
+  h, w = shape[:2]
+  cx = (np.arange(w) + 0.5) / w
+  cy = (np.arange(h) + 0.5) / h
+  gx, gy = np.meshgrid(np.concatenate([cx, [0.0, 1.0]]), np.concatenate([cy, [0.0, 1.0]]))
+  uv = np.concatenate([uv, np.stack([gx, gy], -1).reshape(-1, 2).astype(np.float32)])
+  ref = texture.texture_map(uv, tex)
+  out = shaders.texture_map(torch.tensor(uv, device=device), torch.tensor(tex, device=device))
+  np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_bilinear_resample_known_answers(device):
+  """image_test.py:26-119 through the kernel (zero padding, texel units)."""
+  n = 64
+  img = np.arange(3 * n * n).reshape(n, n, 3).astype(np.float32)
+  x, y = np.meshgrid(np.arange(n), np.arange(n))
+  loc = (np.stack((x, y), -1) + 0.5).astype(np.float32)
+  out = shaders.bilinear_resample(torch.tensor(img, device=device),
+                                  torch.tensor(loc, device=device))
+  np.testing.assert_array_equal(out.cpu().numpy(), img)
+  g = helpers.golden("texture_cases.npz")
+  h, w = g["shape"]
+  ramp = np.repeat(np.arange(1, w + 1, dtype=np.float32)[None], h, 0)[..., None].repeat(3, 2)
+  out = shaders.bilinear_resample(torch.tensor(ramp, device=device),
+                                  torch.tensor(g["samples"], device=device))
+  np.testing.assert_array_almost_equal(out.cpu().numpy(),
+                                       g["expected"][:, None].repeat(3, 1), decimal=5)
+  ref = texture.bilinear_resample(ramp, g["samples"])
+  np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pad_mode", ["edge", "constant"])
+def test_texture_map_backward_matches_autograd(pad_mode, device):
+  rng = np.random.default_rng(11)
+  tex = rng.uniform(-1, 1, (6, 9, 3)).astype(np.float32)
+  loc = rng.uniform(-1.5, 10.5, (2000, 2)).astype(np.float32) * np.array([1.0, 6.0 / 9.0],
+                                                                          np.float32)
+  g = rng.standard_normal((2000, 3)).astype(np.float32)
+  tl = torch.tensor(loc, dtype=torch.float64, requires_grad=True)
+  tt = torch.tensor(tex, dtype=torch.float64, requires_grad=True)
+  ref = texture.bilinear_resample_t(tt, tl, pad_mode)
+  gl, gt = torch.autograd.grad(ref, (tl, tt), torch.tensor(g, dtype=torch.float64))
+  dl = torch.tensor(loc, device=device, requires_grad=True)
+  dt = torch.tensor(tex, device=device, requires_grad=True)
+  out = shaders.bilinear_resample(dt, dl, pad_mode)
+  ol, ot = torch.autograd.grad(out, (dl, dt), torch.tensor(g, device=device))
+  assert_grad_close(ol.cpu().numpy(), gl.numpy())
+  assert_grad_close(ot.cpu().numpy(), gt.numpy())
+
+
+def test_textured_square_golden(device):
+  """shaders_test.py:33-74: a textured square through render_triangles."""
+  g = helpers.golden("render_goldens.npz")
+  tex = torch.tensor(g["textured_square_texture"], device=device)
+  rendered = render.render_triangles(
+      torch.tensor(g["textured_square_clip"], device=device),
+      {"uv": torch.tensor(g["textured_square_uv"], device=device)},
+      torch.tensor(g["textured_square_triangles"], device=device), None, 640, 480,
+      lambda a: shaders.texture_map(a["uv"], tex))
+  ok, msg = helpers.images_near_python(helpers.to_rgba(g["textured_square"]),
+                                       helpers.pil_format(rendered.cpu().numpy()))
+  assert ok, msg
