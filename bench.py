@@ -49,7 +49,7 @@ def parse():
   ap.add_argument("--steps", type=int, default=100)
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-  ap.add_argument("--workload", default="c5", choices=["c5", "c2", "c3", "c1"])
+  ap.add_argument("--workload", default="c5", choices=["c5", "c2", "c3", "c4", "c1"])
   ap.add_argument("--num-meshes", type=int, default=64)
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--no-plain", action="store_true")
@@ -84,10 +84,23 @@ class Workload:
       cams = [wl.camera_matrix(e, 1024, 1024) for e in eyes]
       sizes = [(1024, 1024)] * 8
       desc = "100k-triangle noisy icosphere, 8 cameras, 1024x1024, L=3, fwd+bwd"
+    elif name == "c4":
+      m = wl.heightfield_workload(708, seed=seed)
+      eyes = wl.sphere_eyes(4, seed=seed + 1, radius=2.2, upper_only=True)
+      meshes = [m] * 4
+      cams = [wl.camera_matrix(e, 2048, 2048) for e in eyes]
+      sizes = [(2048, 2048)] * 4
+      rng = np.random.default_rng(seed + 5)
+      self.texture = rng.integers(0, 256, (1024, 1024, 4)).astype(np.float32) / 255.0
+      desc = ("708x708 heightfield (999,698 triangles) with uv, 1024^2 RGBA texture "
+              "(bilinear, edge clamp), 4 cameras, 2048x2048, L=3, fwd+bwd L2 loss wrt "
+              "vertices and texture")
     else:
       m = wl.icosphere_workload(16, seed=seed)
       meshes, cams, sizes = [m], [wl.camera_matrix((0, 0, 3.0), 256, 256)], [(256, 256)]
       desc = "5120-triangle icosphere, 256x256, L=3, fwd+bwd"
+    if name != "c4":
+      self.texture = None
     self.meshes, self.cams, self.sizes, self.desc = meshes, cams, sizes, desc
     self.num_layers = 3
     self.pixels = int(sum(w * h for w, h in sizes))
@@ -217,9 +230,14 @@ def kernel_bytes(wl, fg, near=None, C=4, K=4):
       # sample and d position of every foreground sample out
       "splat_bwd": near * (12 * (C + 1) + 4 * C) + 4 * S + (16 + 4 * C) * fg + 4 * C * S + 16 * fg,
       # z of every sample; ids, bary, d position and d attributes of the
-      # foreground ones and the mesh in; vertex gradients (clip + attributes)
-      # read and written once
-      "samples_bwd": 4 * S + fg * (16 + 16 + 4 * K) + T * 12 + V * (16 + 4 * K) * 3,
+      # depth of every sample; barycentrics, vertex indices, d position,
+      # position and d attributes of the foreground ones; vertex gradients
+      # (clip + attributes) read and written once
+      "samples_bwd": 4 * S + fg * (12 + 12 + 8 + 16 + 4 * K) + V * (16 + 4 * K) * 3,
+      # texture shader on every sample: uv in, C channels out (texels from L2)
+      "texture_fwd": S * (8 + 4 * C),
+      # its VJP: d color and uv in, d uv out (texture gradient atomics in L2)
+      "texture_bwd": S * (4 * C + 8 + 8),
   }
 
 
@@ -249,8 +267,16 @@ def run_ours(args, rank, world, device):
   r = batch_lib.BatchRenderer([m.triangles for m in wl.meshes],
                               [len(m.vertices) for m in wl.meshes], wl.sizes,
                               num_layers=wl.num_layers, device=device, tile="auto")
+  from diffren_gb300 import shaders
+  textured = wl.texture is not None
   verts_h = torch.from_numpy(np.concatenate([m.vertices for m in wl.meshes])).pin_memory()
-  cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
+  # The optimized parameters besides the vertices: per-vertex RGB, or the
+  # texture of a textured workload (whose uvs are a fixed input).
+  if textured:
+    cols_h = torch.from_numpy(wl.texture).pin_memory()
+    uv = torch.from_numpy(np.concatenate([m.uvs for m in wl.meshes])).to(device)
+  else:
+    cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
   cams_h = torch.from_numpy(np.stack(wl.cams)).pin_memory()
   target = torch.from_numpy(np.concatenate([t.reshape(-1, 4) for t in wl.targets])).to(device)
   verts = verts_h.to(device)
@@ -263,7 +289,10 @@ def run_ours(args, rank, world, device):
   def step():
     v = verts.detach().requires_grad_(True)
     c = cols.detach().requires_grad_(True)
-    out = r.render(v, {"rgba": rgba(c)}, cams, shader)
+    if textured:
+      out = r.render(v, {"uv": uv}, cams, lambda a: shaders.texture_map(a["uv"], c))
+    else:
+      out = r.render(v, {"rgba": rgba(c)}, cams, shader)
     loss = l2_loss(out, target)
     gv, gc = torch.autograd.grad(loss, (v, c))
     g_v.copy_(gv)
@@ -355,20 +384,29 @@ def run_plain(wl, device, args):
   """64 separate per-mesh renders (eager), same loss and gradients."""
   import torch
   from diffren_gb300 import render
+  from diffren_gb300 import shaders
+  textured = wl.texture is not None
+  tex = torch.tensor(wl.texture, device=device) if textured else None
   data = []
   for m, cam, (w, h), t in zip(wl.meshes, wl.cams, wl.sizes, wl.targets):
     data.append((torch.tensor(m.vertices, device=device),
-                 torch.tensor(m.colors, device=device),
+                 tex if textured else torch.tensor(m.colors, device=device),
+                 torch.tensor(m.uvs, device=device) if textured else None,
                  torch.tensor(m.triangles, device=device),
                  torch.tensor(cam, device=device), w, h,
                  torch.tensor(t, device=device)))
 
   def step():
-    for v0, c0, tri, cam, w, h, tgt in data:
+    for v0, c0, uv, tri, cam, w, h, tgt in data:
       v = v0.detach().requires_grad_(True)
       c = c0.detach().requires_grad_(True)
-      out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
-                                    num_layers=wl.num_layers)
+      if textured:
+        out = render.render_triangles(v, {"uv": uv}, tri, cam, w, h,
+                                      lambda a: shaders.texture_map(a["uv"], c),
+                                      num_layers=wl.num_layers)
+      else:
+        out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
+                                      num_layers=wl.num_layers)
       loss = l2_loss(out, tgt)
       torch.autograd.grad(loss, (v, c))
 
@@ -401,8 +439,9 @@ def cpu_port_sample(wl, budget_s, threads, images=None):
   """
   import concurrent.futures
   import torch
-  from oracle import raster, torch_ref
+  from oracle import raster, texture, torch_ref
   torch.set_num_threads(threads)
+  ttex = None if wl.texture is None else torch.tensor(wl.texture, requires_grad=True)
   order = list(images) if images is not None else list(range(len(wl.meshes)))
 
   def rasterize(i):
@@ -422,12 +461,17 @@ def cpu_port_sample(wl, budget_s, threads, images=None):
         m, (w, h), tgt = wl.meshes[i], wl.sizes[i], wl.targets[i]
         state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
         tc = torch.tensor(clip, requires_grad=True)
-        tcol = torch.tensor(m.colors, requires_grad=True)
         ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
-        shaded = torch_ref.interpolate(rgba(tcol), ti, tz, tb, tt)
+        if ttex is not None:
+          tparam = ttex
+          uvs = torch_ref.interpolate(torch.tensor(m.uvs), ti, tz, tb, tt)
+          shaded = texture.texture_map_t(uvs, ttex)
+        else:
+          tparam = torch.tensor(m.colors, requires_grad=True)
+          shaded = torch_ref.interpolate(rgba(tparam), ti, tz, tb, tt)
         out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
         loss = l2_loss(out, torch.tensor(tgt))
-        torch.autograd.grad(loss, (tc, tcol))
+        torch.autograd.grad(loss, (tc, tparam))
         px += w * h
         used += 1
       t_total += time.perf_counter() - t0
@@ -510,7 +554,7 @@ def main():
     return
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
-  nbytes = kernel_bytes(wl, res["fg"], res["near"])
+  nbytes = kernel_bytes(wl, res["fg"], res["near"], K=2 if wl.texture is not None else 4)
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
   value = whole_job_mpix(world, wl.pixels, res["ms"])

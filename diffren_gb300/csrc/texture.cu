@@ -112,9 +112,29 @@ __global__ void __launch_bounds__(256) texture_bwd_kernel(TexArgs a) {
   }
   const Footprint f = footprint(a, i);
   float du = 0.0f, dv = 0.0f;
+  if (a.d_tex && (a.C & 3) == 0 && (reinterpret_cast<uintptr_t>(a.d_tex) & 15) == 0) {
+    // Four channels per vector atomic.
+    const float w00 = f.r.fw * f.c.fw, w10 = f.r.cw * f.c.fw, w11 = f.r.cw * f.c.cw,
+                w01 = f.r.fw * f.c.cw;
+    for (int k = 0; k < a.C; k += 4) {
+      const float4 gk = make_float4(__ldg(g + k), __ldg(g + k + 1), __ldg(g + k + 2),
+                                    __ldg(g + k + 3));
+      const auto add = [&](int64_t t, float w) {
+        if (t >= 0)
+          atomicAdd(reinterpret_cast<float4*>(a.d_tex + t + k),
+                    make_float4(gk.x * w, gk.y * w, gk.z * w, gk.w * w));
+      };
+      add(f.t00, w00);
+      add(f.t10, w10);
+      add(f.t11, w11);
+      add(f.t01, w01);
+    }
+  }
+  const bool scalar_tex = a.d_tex && !((a.C & 3) == 0 &&
+                                       (reinterpret_cast<uintptr_t>(a.d_tex) & 15) == 0);
   for (int k = 0; k < a.C; ++k) {
     const float gk = __ldg(g + k);
-    if (a.d_tex && gk != 0.0f) {
+    if (scalar_tex && gk != 0.0f) {
       if (f.t00 >= 0) atomicAdd(a.d_tex + f.t00 + k, gk * f.r.fw * f.c.fw);
       if (f.t10 >= 0) atomicAdd(a.d_tex + f.t10 + k, gk * f.r.cw * f.c.fw);
       if (f.t11 >= 0) atomicAdd(a.d_tex + f.t11 + k, gk * f.r.cw * f.c.cw);
