@@ -98,9 +98,13 @@ class Workload:
     else:
       m = wl.icosphere_workload(16, seed=seed)
       meshes, cams, sizes = [m], [wl.camera_matrix((0, 0, 3.0), 256, 256)], [(256, 256)]
-      desc = "5120-triangle icosphere, 256x256, L=3, fwd+bwd"
+      desc = ("5120-triangle icosphere, 256x256, L=3, point light (2,2,2) on area-weighted "
+              "vertex normals, fwd+bwd L2 loss wrt vertices and RGB")
     if name != "c4":
       self.texture = None
+    # Lit workloads shade with shaders.point_light on vertex normals
+    # recomputed from the vertices every step.
+    self.lit = name == "c1"
     self.meshes, self.cams, self.sizes, self.desc = meshes, cams, sizes, desc
     self.num_layers = 3
     self.pixels = int(sum(w * h for w, h in sizes))
@@ -116,6 +120,22 @@ def shader(a):
   """Pass-through of the interpolated RGBA vertex colors (the reference's
   render tests shade with `lambda x: x['rgba']` the same way)."""
   return a["rgba"]
+
+
+LIGHT = (2.0, 2.0, 2.0)
+
+
+def lit_shader(a):
+  """point_light (shaders.py:100-173) with default coefficients on the
+  interpolated RGB, normals and world positions; alpha 1."""
+  from diffren_gb300 import shaders
+  rgb = shaders.point_light(a["rgb"], a["normals"], a["pos"], LIGHT)
+  return torch_cat_alpha(rgb)
+
+
+def torch_cat_alpha(rgb):
+  import torch
+  return torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
 
 
 def rgba(colors):
@@ -291,6 +311,9 @@ def run_ours(args, rank, world, device):
     c = cols.detach().requires_grad_(True)
     if textured:
       out = r.render(v, {"uv": uv}, cams, lambda a: shaders.texture_map(a["uv"], c))
+    elif wl.lit:
+      out = r.render(v, {"rgb": c, "normals": r.vertex_normals(v), "pos": v}, cams,
+                     lit_shader)
     else:
       out = r.render(v, {"rgba": rgba(c)}, cams, shader)
     loss = l2_loss(out, target)
@@ -383,7 +406,7 @@ def run_ours(args, rank, world, device):
 def run_plain(wl, device, args):
   """64 separate per-mesh renders (eager), same loss and gradients."""
   import torch
-  from diffren_gb300 import render
+  from diffren_gb300 import mesh, render
   from diffren_gb300 import shaders
   textured = wl.texture is not None
   tex = torch.tensor(wl.texture, device=device) if textured else None
@@ -403,6 +426,10 @@ def run_plain(wl, device, args):
       if textured:
         out = render.render_triangles(v, {"uv": uv}, tri, cam, w, h,
                                       lambda a: shaders.texture_map(a["uv"], c),
+                                      num_layers=wl.num_layers)
+      elif wl.lit:
+        attrs = {"rgb": c, "normals": mesh.compute_vertex_normals(v, tri), "pos": v}
+        out = render.render_triangles(v, attrs, tri, cam, w, h, lit_shader,
                                       num_layers=wl.num_layers)
       else:
         out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
@@ -439,6 +466,7 @@ def cpu_port_sample(wl, budget_s, threads, images=None):
   """
   import concurrent.futures
   import torch
+  from oracle import mesh as omesh
   from oracle import raster, texture, torch_ref
   torch.set_num_threads(threads)
   ttex = None if wl.texture is None else torch.tensor(wl.texture, requires_grad=True)
@@ -462,16 +490,28 @@ def cpu_port_sample(wl, budget_s, threads, images=None):
         state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
         tc = torch.tensor(clip, requires_grad=True)
         ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
+        tv = tc
+        if wl.lit:
+          # Clip vertices from world vertices in torch, so that the
+          # gradient reaches the vertices through the normals too.
+          tv = torch.tensor(m.vertices, requires_grad=True)
+          cam = torch.tensor(wl.cams[i], dtype=torch.float32)
+          tc = torch.cat([tv, torch.ones_like(tv[:, :1])], 1) @ cam.T
         if ttex is not None:
           tparam = ttex
           uvs = torch_ref.interpolate(torch.tensor(m.uvs), ti, tz, tb, tt)
           shaded = texture.texture_map_t(uvs, ttex)
+        elif wl.lit:
+          tparam = torch.tensor(m.colors, requires_grad=True)
+          attrs = torch.cat([tparam, omesh.vertex_normals_t(tv, tt), tv], 1)
+          a = torch_ref.interpolate(attrs, ti, tz, tb, tt)
+          shaded = lit_shader({"rgb": a[..., :3], "normals": a[..., 3:6], "pos": a[..., 6:9]})
         else:
           tparam = torch.tensor(m.colors, requires_grad=True)
           shaded = torch_ref.interpolate(rgba(tparam), ti, tz, tb, tt)
         out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
         loss = l2_loss(out, torch.tensor(tgt))
-        torch.autograd.grad(loss, (tc, tparam))
+        torch.autograd.grad(loss, (tv, tparam))
         px += w * h
         used += 1
       t_total += time.perf_counter() - t0

@@ -71,6 +71,12 @@ class BatchRenderer:
     self._autotune = False
     return choice
 
+  def vertex_normals(self, vertices):
+    """Area-weighted unit normals (mesh.py:22-52) of every mesh of the batch
+    from packed world vertices [sum V, 3]; differentiable."""
+    from . import mesh
+    return mesh.vertex_normals_packed(vertices, self.triangles, self.batch)
+
   @property
   def num_images(self):
     return self.batch.n

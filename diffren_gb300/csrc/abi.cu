@@ -259,6 +259,25 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                 err);
 }
 
+int dr_vertex_normals_fwd(const float* vertices, const int32_t* triangles,
+                          const dr_image_desc* meshes, int32_t num_meshes, float* accum,
+                          float* normals, void* stream) {
+  std::string err;
+  return finish(dr::normals_fwd_launch(vertices, triangles, meshes, num_meshes, accum, normals,
+                                       as_stream(stream), err),
+                err);
+}
+
+int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
+                          const int32_t* triangles, const dr_image_desc* meshes,
+                          int32_t num_meshes, const float* accum, float* d_accum,
+                          float* d_vertices, void* stream) {
+  std::string err;
+  return finish(dr::normals_bwd_launch(d_normals, vertices, triangles, meshes, num_meshes,
+                                       accum, d_accum, d_vertices, as_stream(stream), err),
+                err);
+}
+
 int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
                            const int32_t* triangle_ids, const float* z_buffer,
                            const float* barycentrics, const dr_image_desc* images,

@@ -108,6 +108,15 @@ int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const flo
                        int H, int W, int C, int flags, float* d_uv, float* d_tex,
                        cudaStream_t stream, std::string& err);
 
+// normals.cu
+int normals_fwd_launch(const float* vertices, const int32_t* tris, const dr_image_desc* images,
+                       int n, float* accum, float* normals, cudaStream_t stream,
+                       std::string& err);
+int normals_bwd_launch(const float* d_normals, const float* vertices, const int32_t* tris,
+                       const dr_image_desc* images, int n, const float* accum,
+                       float* d_accum, float* d_vertices, cudaStream_t stream,
+                       std::string& err);
+
 // splat.cu
 int samples_fwd_launch(const float* attributes, int K, const float* clip,
                        const int32_t* tris, const int32_t* ids, const float* z,

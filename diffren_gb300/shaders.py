@@ -4,7 +4,10 @@ diffren/jax/utils/image.py).
 ``texture_map`` is the reference's bilinear texture lookup with edge
 clamping (shaders.py:40-65) and ``bilinear_resample`` the resampler under it
 (image.py:21-118), as one CUDA kernel with a hand-written VJP to the
-coordinates and the image. Any torch function remains usable as a shader.
+coordinates and the image. ``diffuse_light`` and ``point_light``
+(shaders.py:68-173) are the reference's lighting formulas as elementwise
+torch expressions on the interpolated buffers. Any torch function remains
+usable as a shader.
 """
 import torch
 
@@ -77,3 +80,52 @@ def bilinear_resample(image, locations, pad_mode="constant"):
   flags = _lib.DR_TEXTURE_TEXEL_UNITS | (_lib.DR_TEXTURE_PAD_ZERO if pad_mode == "constant"
                                          else 0)
   return _resample(locations, image, flags)
+
+
+def _vec3(v, like):
+  """v (a tensor or three numbers) as a tensor like `like`; numbers are
+  written with device-side fills, so that this works under CUDA graph
+  capture."""
+  if torch.is_tensor(v):
+    return v.to(dtype=like.dtype, device=like.device)
+  out = like.new_empty(3)
+  for i, x in enumerate(v):
+    out.narrow(0, i, 1).fill_(float(x))
+  return out
+
+
+def l2_normalize(x, dim=-1, eps=1e-12):
+  """transforms.l2_normalize (transforms.py:26-37): x * rsqrt(|x|^2 + eps)."""
+  return x * torch.rsqrt((x * x).sum(dim=dim, keepdim=True) + eps)
+
+
+def diffuse_light(diffuse_image, normals_image, light_direction=(0.5, 0.5, 1.0), ka=0.5,
+                  kd=0.5):
+  """shaders.diffuse_light (shaders.py:68-97): ambient plus directional
+  diffuse, diffuse * (ka + kd * clip(n . l, 0, 1)) with l normalized."""
+  d = _vec3(light_direction, normals_image)
+  d = l2_normalize(d.reshape(*([1] * (normals_image.dim() - 1)), 3))
+  n_dot_l = (normals_image * d).sum(-1, keepdim=True).clamp(0.0, 1.0)
+  return diffuse_image * ka + diffuse_image * kd * n_dot_l
+
+
+def point_light(diffuse_image, normals_image, pixel_positions, point_locations,
+                eye_position=(0.0, 0.0, 0.0), ka=0.3, kd=1.4, ks=0.0, ns=0.0,
+                attenuation_constant=1.0, attenuation_linear=0.7,
+                attenuation_quadratic=1.8):
+  """shaders.point_light (shaders.py:100-173): a point light with ambient,
+  diffuse and Blinn-Phong specular terms and quadratic distance attenuation
+  1 / (c + l d + q d^2); images are [..., 3]."""
+  light = _vec3(point_locations, pixel_positions)
+  eye = _vec3(eye_position, pixel_positions)
+  to_light = light - pixel_positions
+  light_dir = l2_normalize(to_light)
+  view_dir = l2_normalize(eye - pixel_positions)
+  half = l2_normalize(light_dir + view_dir)
+  nol = (normals_image * light_dir).sum(-1, keepdim=True).clamp(0.0, 1.0)
+  noh = (normals_image * half).sum(-1, keepdim=True).clamp(0.0, 1.0)
+  dist = torch.linalg.vector_norm(to_light, dim=-1, keepdim=True)
+  decay = 1.0 / (attenuation_constant + attenuation_linear * dist +
+                 attenuation_quadratic * dist * dist)
+  luma = ka + kd * nol + ks * noh ** ns
+  return diffuse_image * luma * decay

@@ -40,6 +40,8 @@
  *       transform of splat.splat_shaded_pixels (splat.py:207-221) and its VJP.
  *   dr_texture_map_fwd/bwd  -> utils.shaders.texture_map
  *       (diffren/jax/utils/shaders.py:40-65, utils/image.py:21-118).
+ *   dr_vertex_normals_fwd/bwd -> utils.mesh.compute_vertex_normals
+ *       (diffren/jax/utils/mesh.py:22-52) and its VJP.
  *   dr_splat_fwd/bwd        -> splat.splat_at_pixel_centers + composite.over
  *       (diffren/jax/internal/splat.py:26-175, diffren/jax/composite.py:20-37)
  *       and their VJP.
@@ -319,6 +321,29 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                        const float* texture, int32_t height, int32_t width,
                        int32_t channels, int32_t flags, float* d_uv, float* d_texture,
                        void* stream);
+
+/* ------------------------------------------------------------- meshes */
+
+/* mesh.compute_vertex_normals (diffren/jax/utils/mesh.py:22-52) over a
+ * ragged batch of meshes, one per descriptor (only num_vertices,
+ * num_triangles, vertex_offset and triangle_offset are read): face normals
+ * cross(v1 - v0, v2 - v0) summed into each corner vertex, then
+ * x * rsqrt(|x|^2 + 1e-12) (transforms.l2_normalize, transforms.py:26-37).
+ * vertices [V, 3], normals [V, 3], accum [V, 4] scratch (16-byte aligned)
+ * that the VJP reads back; V = max(vertex_offset + num_vertices).
+ * Triangles with an out-of-range index add nothing. Meshes are disjoint
+ * vertex ranges: a vertex covered by two descriptors sums both. The sums
+ * use float atomics, so their order (and the last bits) varies by run. */
+int dr_vertex_normals_fwd(const float* vertices, const int32_t* triangles,
+                          const dr_image_desc* meshes, int32_t num_meshes, float* accum,
+                          float* normals, void* stream);
+
+/* Its VJP: d_accum [V, 4] scratch (16-byte aligned), d_vertices [V, 3]
+ * accumulated (caller zeroes it). */
+int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
+                          const int32_t* triangles, const dr_image_desc* meshes,
+                          int32_t num_meshes, const float* accum, float* d_accum,
+                          float* d_vertices, void* stream);
 
 /* splat_at_pixel_centers + composite.over (splat.py:26-175,
  * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the

@@ -265,3 +265,34 @@ def test_texture_oracle_torch_matches_numpy_and_finite_differences():
   u = torch.tensor(uv, dtype=torch.float64, requires_grad=True)
   assert torch.autograd.gradcheck(lambda uu, tt: texture.texture_map_t(uu, tt), (u, t),
                                   eps=1e-6, atol=1e-5)
+
+
+def _sphere():
+  g = helpers.golden("render_goldens.npz")
+  return g["sphere_vertices"].astype(np.float32), g["sphere_triangles"].astype(np.int64)
+
+
+def test_vertex_normals_oracle_sphere_known_answers():
+  """mesh_test.py:32-80: a unit sphere's normals are its vertices; stretching
+  z by 2 halves the normals' z before renormalizing."""
+  from oracle import mesh
+  v, t = _sphere()
+  np.testing.assert_array_almost_equal(v, mesh.vertex_normals(v, t), decimal=2)
+  s = v.copy()
+  s[:, 2] *= 2.0
+  want = v.copy()
+  want[:, 2] *= 0.5
+  want /= np.linalg.norm(want, axis=1, keepdims=True)
+  np.testing.assert_array_almost_equal(want, mesh.vertex_normals(s, t), decimal=2)
+
+
+def test_vertex_normals_torch_oracle_matches_numpy_and_finite_differences():
+  from oracle import mesh
+  v, t = _sphere()
+  rng = np.random.default_rng(5)
+  v = v + rng.normal(0, 0.05, v.shape).astype(np.float32)
+  tv = torch.tensor(v, dtype=torch.float64, requires_grad=True)
+  tt = torch.tensor(t)
+  np.testing.assert_allclose(mesh.vertex_normals_t(tv, tt).detach().numpy(),
+                             mesh.vertex_normals(v, t), rtol=1e-12, atol=1e-12)
+  assert torch.autograd.gradcheck(lambda x: mesh.vertex_normals_t(x, tt), (tv,))
