@@ -372,22 +372,60 @@ def run_ours(args, rank, world, device):
   clock = clocks.summary(start)
   loss_val = float(loss_out)
 
-  # e2e: public API with host buffers; H2D inputs and D2H loss + grads.
+  # e2e: public API with host buffers. Every step copies its inputs from
+  # pinned host memory and its loss and gradients back. The copies run on
+  # two copy streams through staging buffers in HBM, so that step i+1's
+  # inputs arrive and step i-1's gradients leave while step i computes; the
+  # timed region runs from before the first input copy to the end of the
+  # last gradient copy.
   gv_h = torch.empty_like(verts_h).pin_memory()
   gc_h = torch.empty_like(cols_h).pin_memory()
   loss_h = torch.empty((), pin_memory=True)
+  h2d_s = torch.cuda.Stream(device)
+  d2h_s = torch.cuda.Stream(device)
+  stage_in = [torch.empty_like(x) for x in (verts, cols, cams)]
+  stage_out = [torch.empty_like(x) for x in (g_v, g_c, loss_out)]
 
-  def e2e_step():
-    verts.copy_(verts_h, non_blocking=True)
-    cols.copy_(cols_h, non_blocking=True)
-    cams.copy_(cams_h, non_blocking=True)
-    graph.replay()
-    gv_h.copy_(g_v, non_blocking=True)
-    gc_h.copy_(g_c, non_blocking=True)
-    loss_h.copy_(loss_out, non_blocking=True)
+  def e2e_steps(k):
+    cur = torch.cuda.current_stream(device)
+    in_ready, in_free = torch.cuda.Event(), torch.cuda.Event()
+    out_ready, out_free = torch.cuda.Event(), torch.cuda.Event()
 
-  e2e_step()
-  ms_e2e = timed(e2e_step, args.steps)
+    def upload():
+      with torch.cuda.stream(h2d_s):
+        for dst, src in zip(stage_in, (verts_h, cols_h, cams_h)):
+          dst.copy_(src, non_blocking=True)
+        in_ready.record(h2d_s)
+
+    h2d_s.wait_stream(cur)
+    upload()
+    for i in range(k):
+      cur.wait_event(in_ready)
+      for dst, src in zip((verts, cols, cams), stage_in):
+        dst.copy_(src)
+      in_free.record(cur)
+      if i + 1 < k:
+        h2d_s.wait_event(in_free)
+        upload()
+      graph.replay()
+      if i > 0:
+        cur.wait_event(out_free)
+      for dst, src in zip(stage_out, (g_v, g_c, loss_out)):
+        dst.copy_(src)
+      out_ready.record(cur)
+      d2h_s.wait_event(out_ready)
+      with torch.cuda.stream(d2h_s):
+        for dst, src in zip((gv_h, gc_h, loss_h), stage_out):
+          dst.copy_(src, non_blocking=True)
+        out_free.record(d2h_s)
+    cur.wait_stream(d2h_s)
+
+  e2e_steps(2)
+  torch.cuda.synchronize(device)
+  ms_e2e = timed(lambda: e2e_steps(args.steps), 1) / args.steps
+  if abs(float(loss_h) - loss_val) > 1e-4 * abs(loss_val):
+    print("warning: e2e loss %r differs from the graph's %r" % (float(loss_h), loss_val),
+          file=sys.stderr)
   h2d = verts_h.numel() * 4 + cols_h.numel() * 4 + cams_h.numel() * 4
   d2h = gv_h.numel() * 4 + gc_h.numel() * 4 + 4
 
