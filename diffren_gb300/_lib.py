@@ -74,6 +74,8 @@ SIGNATURES = {
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_texture_map_fwd": (_I, [_P, _L, _P, _I, _I, _I, _I, _P, _P]),
     "dr_texture_map_bwd": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P]),
+    "dr_composite_over_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P]),
+    "dr_composite_over_bwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_vertex_normals_fwd": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "dr_vertex_normals_bwd": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),

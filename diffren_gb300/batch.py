@@ -137,19 +137,9 @@ class BatchRenderer:
     shaded = shaded.reshape(-1, shaded.shape[-1])
     if splatting:
       return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers, z=z)
-    fg = (z != 1.0).float()[:, None]
-    shaded = shaded * fg
     if compositing_mode == constants.CompositingMode.NONE:
-      return shaded
-    # OVER: composite each image's layers (front to back).
-    outs = []
-    for i in range(b.n):
-      lay = b.layered_view(shaded, i, L)
-      out = lay[-1]
-      for l in range(L - 2, -1, -1):
-        out = lay[l] + (1.0 - lay[l, ..., -1:]) * out
-      outs.append(out.reshape(-1, out.shape[-1]))
-    return torch.cat(outs)
+      return shaded * (z != 1.0).float()[:, None]
+    return kernels.over_packed(shaded, z, b, L)
 
   def images(self, packed):
     """List of [H_i, W_i, C] views of a packed composited result."""

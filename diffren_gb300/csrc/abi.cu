@@ -259,6 +259,24 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                 err);
 }
 
+int dr_composite_over_fwd(const float* shaded, const float* z_buffer, int32_t channels,
+                          const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                          float* out, void* stream) {
+  std::string err;
+  return finish(dr::over_fwd_launch(shaded, z_buffer, channels, images, num_images, num_layers,
+                                    out, as_stream(stream), err),
+                err);
+}
+
+int dr_composite_over_bwd(const float* d_out, const float* shaded, const float* z_buffer,
+                          int32_t channels, const dr_image_desc* images, int32_t num_images,
+                          int32_t num_layers, float* d_shaded, void* stream) {
+  std::string err;
+  return finish(dr::over_bwd_launch(d_out, shaded, z_buffer, channels, images, num_images,
+                                    num_layers, d_shaded, as_stream(stream), err),
+                err);
+}
+
 int dr_vertex_normals_fwd(const float* vertices, const int32_t* triangles,
                           const dr_image_desc* meshes, int32_t num_meshes, float* accum,
                           float* normals, void* stream) {

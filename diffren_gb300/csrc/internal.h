@@ -108,6 +108,13 @@ int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const flo
                        int H, int W, int C, int flags, float* d_uv, float* d_tex,
                        cudaStream_t stream, std::string& err);
 
+// composite.cu
+int over_fwd_launch(const float* shaded, const float* z, int C, const dr_image_desc* images,
+                    int n, int L, float* out, cudaStream_t stream, std::string& err);
+int over_bwd_launch(const float* d_out, const float* shaded, const float* z, int C,
+                    const dr_image_desc* images, int n, int L, float* d_shaded,
+                    cudaStream_t stream, std::string& err);
+
 // normals.cu
 int normals_fwd_launch(const float* vertices, const int32_t* tris, const dr_image_desc* images,
                        int n, float* accum, float* normals, cudaStream_t stream,

@@ -617,3 +617,45 @@ def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=Fals
   if z is not None:
     z = z.detach().contiguous()
   return _Splat.apply(positions, colors, z, batch, num_layers, bool(return_accum_buffers))
+
+
+class _Over(torch.autograd.Function):
+
+  @staticmethod
+  def forward(ctx, shaded, z, batch, num_layers):
+    lib = _lib.load()
+    C = shaded.shape[1]
+    out = torch.empty(batch.total_pixels, C, dtype=torch.float32, device=shaded.device)
+    with _op("composite_over", _groups(batch)):
+      rc = lib.dr_composite_over_fwd(_p(shaded), _p(z), C, batch.ptr, batch.n, num_layers,
+                                     _p(out), _stream(shaded.device))
+    _lib.check(rc, "dr_composite_over_fwd")
+    ctx.save_for_backward(shaded, z)
+    ctx.batch, ctx.L = batch, num_layers
+    return out
+
+  @staticmethod
+  def backward(ctx, d_out):
+    shaded, z = ctx.saved_tensors
+    if not ctx.needs_input_grad[0]:
+      return None, None, None, None
+    lib = _lib.load()
+    d_shaded = torch.empty_like(shaded)
+    with _op("composite_over_bwd", _groups(ctx.batch)):
+      rc = lib.dr_composite_over_bwd(_p(d_out.contiguous()), _p(shaded), _p(z),
+                                     shaded.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L,
+                                     _p(d_shaded), _stream(d_out.device))
+    _lib.check(rc, "dr_composite_over_bwd")
+    return d_shaded, None, None, None
+
+
+def over_packed(shaded, z, batch, num_layers):
+  """CompositingMode.OVER of a packed batch (render.py:134-140): shaded
+  [L*P, C] (alpha last) times the foreground mask z != 1, composited front
+  to back per pixel (composite.py:20-37). Returns [P, C]; differentiable
+  w.r.t. shaded."""
+  _require_cuda(shaded, z)
+  shaded = shaded.contiguous()
+  if shaded.dtype != torch.float32:
+    shaded = shaded.float()
+  return _Over.apply(shaded, z.detach().contiguous(), batch, int(num_layers))

@@ -15,7 +15,6 @@ from typing import Callable, Dict
 
 import torch
 
-from . import composite
 from . import constants
 from . import interpolate
 from . import kernels
@@ -108,9 +107,11 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   if compositing_mode == constants.CompositingMode.SPLAT_OVER:
     return splat.splat_clip(geom.clip, frame, shaded, return_accum_buffers)
 
-  shaded = shaded * frame.foreground_mask
   if compositing_mode == constants.CompositingMode.OVER:
-    if geom.batched:
-      return torch.stack([composite.over(s) for s in shaded])
-    return composite.over(shaded)
-  return shaded
+    # Foreground mask and composite.over in one kernel.
+    C = shaded.shape[-1]
+    out = kernels.over_packed(shaded.reshape(-1, C), frame.z_buffer.reshape(-1), geom.batch,
+                              num_layers)
+    lead = (geom.B,) if geom.batched else ()
+    return out.view(*lead, image_height, image_width, C)
+  return shaded * frame.foreground_mask

@@ -40,6 +40,9 @@
  *       transform of splat.splat_shaded_pixels (splat.py:207-221) and its VJP.
  *   dr_texture_map_fwd/bwd  -> utils.shaders.texture_map
  *       (diffren/jax/utils/shaders.py:40-65, utils/image.py:21-118).
+ *   dr_composite_over_fwd/bwd -> the OVER mode of render.render_triangles
+ *       (diffren/jax/render.py:134-140: foreground mask, composite.over of
+ *       composite.py:20-37) and its VJP.
  *   dr_vertex_normals_fwd/bwd -> utils.mesh.compute_vertex_normals
  *       (diffren/jax/utils/mesh.py:22-52) and its VJP.
  *   dr_splat_fwd/bwd        -> splat.splat_at_pixel_centers + composite.over
@@ -321,6 +324,23 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                        const float* texture, int32_t height, int32_t width,
                        int32_t channels, int32_t flags, float* d_uv, float* d_texture,
                        void* stream);
+
+/* ------------------------------------------------------ compositing */
+
+/* CompositingMode.OVER of render_triangles (render.py:134-140): shaded
+ * [L, H, W, C] per image (alpha in the last channel, premultiplied) times
+ * the foreground mask (z_buffer [L, H, W] != 1), composited back to front,
+ * o = s[L-1]; o = s[l] + (1 - alpha[l]) * o (composite.py:20-37), into out
+ * [H, W, C] per image. Channels >= 1, 1 <= num_layers <= DR_MAX_LAYERS. */
+int dr_composite_over_fwd(const float* shaded, const float* z_buffer, int32_t channels,
+                          const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                          float* out, void* stream);
+
+/* Its VJP: d_shaded [L, H, W, C] per image is written (background samples
+ * get 0). */
+int dr_composite_over_bwd(const float* d_out, const float* shaded, const float* z_buffer,
+                          int32_t channels, const dr_image_desc* images, int32_t num_images,
+                          int32_t num_layers, float* d_shaded, void* stream);
 
 /* ------------------------------------------------------------- meshes */
 

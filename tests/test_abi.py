@@ -103,11 +103,15 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
                           None, None, None) == 4
   assert lib.dr_splat_positions_fwd(ctypes.c_void_p(4), None, None, None, None, b.ptr, 1,
                                     3, None, None) == 4
+  fake = ctypes.c_void_p(256)
+  # OVER compositing: layer and channel counts, null buffers.
+  assert lib.dr_composite_over_fwd(fake, fake, 4, b.ptr, 1, 0, fake, None) == 1
+  assert lib.dr_composite_over_fwd(fake, fake, 0, b.ptr, 1, 3, fake, None) == 1
+  assert lib.dr_composite_over_bwd(None, fake, fake, 4, b.ptr, 1, 3, fake, None) == 1
   # Vertex normals: null mesh, negative counts, misaligned scratch.
   assert lib.dr_vertex_normals_fwd(None, None, b.ptr, 1, None, None, None) == 1
   neg = kernels.ImageBatch.single(8, 8, 3, 1)
   neg.descs[0].num_triangles = -1
-  fake = ctypes.c_void_p(256)
   assert lib.dr_vertex_normals_fwd(fake, fake, neg.ptr, 1, fake, fake, None) == 1
   assert lib.dr_vertex_normals_fwd(fake, fake, b.ptr, 1, ctypes.c_void_p(260), fake,
                                    None) == 4
