@@ -87,14 +87,15 @@ class Workload:
     elif name == "c4":
       m = wl.heightfield_workload(708, seed=seed)
       eyes = wl.sphere_eyes(4, seed=seed + 1, radius=2.2, upper_only=True)
-      meshes = [m] * 4
-      cams = [wl.camera_matrix(e, 2048, 2048) for e in eyes]
-      sizes = [(2048, 2048)] * 4
+      k = max(1, min(4, num_meshes))  # fewer cameras for small profiling runs
+      meshes = [m] * k
+      cams = [wl.camera_matrix(e, 2048, 2048) for e in eyes[:k]]
+      sizes = [(2048, 2048)] * k
       rng = np.random.default_rng(seed + 5)
       self.texture = rng.integers(0, 256, (1024, 1024, 4)).astype(np.float32) / 255.0
       desc = ("708x708 heightfield (999,698 triangles) with uv, 1024^2 RGBA texture "
-              "(bilinear, edge clamp), 4 cameras, 2048x2048, L=3, fwd+bwd L2 loss wrt "
-              "vertices and texture")
+              "(bilinear, edge clamp), %d cameras, 2048x2048, L=3, fwd+bwd L2 loss wrt "
+              "vertices and texture" % k)
     else:
       m = wl.icosphere_workload(16, seed=seed)
       meshes, cams, sizes = [m], [wl.camera_matrix((0, 0, 3.0), 256, 256)], [(256, 256)]

@@ -125,16 +125,19 @@ __device__ __forceinline__ void tile_rect(int4 box, int TW, int TH, int& tx0,
 // coverage cull, per-tile counts (small triangles) or the large list.
 __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
   const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (g >= a.total_tris) return;
-  const int img = find_segment(B.tri_start, B.n, g);
+  const int lane = threadIdx.x & 31;
+  // Lanes past the end still take part in the warp-wide tile match below.
+  const bool live = g < a.total_tris;
+  const int img = live ? find_segment(B.tri_start, B.n, g) : 0;
   const int64_t t = g - B.tri_start[img];
   const int W = B.width[img], H = B.height[img];
   const int32_t* tri = a.tris + 3 * (B.triangle_offset[img] + t);
-  const int i0 = tri[0], i1 = tri[1], i2 = tri[2];
+  const int i0 = live ? tri[0] : 0, i1 = live ? tri[1] : 0, i2 = live ? tri[2] : 0;
   const unsigned nv = unsigned(B.num_vertices[img]);
   int4 box = make_int4(0, 0, 0, 0);
   bool valid = false;
-  if (unsigned(i0) >= nv || unsigned(i1) >= nv || unsigned(i2) >= nv) {
+  if (!live) {
+  } else if (unsigned(i0) >= nv || unsigned(i1) >= nv || unsigned(i2) >= nv) {
     atomicOr(&a.counters[1], DR_FLAG_INDEX_OUT_OF_RANGE);
   } else {
     const float4* vb = a.verts + B.vertex_offset[img];
@@ -159,13 +162,21 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
     }
   }
   if (!valid) box = make_int4(0, 0, 0, 0);
-  a.bbox[g] = box;
-  if (!valid) return;
-  int tx0, tx1, ty0, ty1;
-  tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
+  if (live) a.bbox[g] = box;
+  int tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1;
+  if (valid) tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
   const int n = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+  const int base = B.tile_start[img], tx = B.tiles_x[img];
+  // Triangles inside one tile count with one atomic per tile per warp.
+  const bool single = valid && n == 1 && n <= a.large_tiles;
+  const int tile0 = base + ty0 * tx + tx0;
+  const unsigned group = __match_any_sync(0xffffffffu, single ? tile0 : -1 - lane);
+  if (single) {
+    if (lane == __ffs(group) - 1) atomicAdd(&a.tile_count[tile0], __popc(group));
+    return;
+  }
+  if (!valid) return;
   if (n <= a.large_tiles) {
-    const int base = B.tile_start[img], tx = B.tiles_x[img];
     for (int y = ty0; y <= ty1; ++y)
       for (int x = tx0; x <= tx1; ++x) atomicAdd(&a.tile_count[base + y * tx + x], 1);
   } else {
@@ -174,34 +185,49 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
   }
 }
 
-// Exclusive scan of the per-tile counts (one block; tiles are few).
+// Exclusive scan of the per-tile counts (one block; tiles are few). A pass
+// covers 16 Ki counts: warp w owns 512 consecutive counts, read 32 at a time
+// with coalesced loads and scanned with warp shuffles, then the 32 warp
+// totals are scanned once; the next pass's counts load meanwhile.
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
                                                          int32_t* first, int n) {
   __shared__ int warp_sums[32];
-  __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  constexpr int kItems = 4;
-  for (int base = 0; base < n; base += 1024 * kItems) {
-    int v[kItems], s = 0;
+  constexpr int kRounds = 16, kChunk = 1024 * kRounds;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int carry = 0;
+  int v[kRounds], next[kRounds];
+  const auto load = [&](int base, int (&dst)[kRounds]) {
 #pragma unroll
-    for (int j = 0; j < kItems; ++j) {
-      const int i = base + threadIdx.x * kItems + j;
-      v[j] = i < n ? count[i] : 0;
-      s += v[j];
+    for (int j = 0; j < kRounds; ++j) {
+      const int i = base + warp * (32 * kRounds) + j * 32 + lane;
+      dst[j] = i < n ? __ldg(count + i) : 0;
     }
-    int excl;
-    const int total = block_exclusive_scan<1024>(s, warp_sums, excl);
-    int run = carry + excl;
+  };
+  load(0, v);
+  for (int base = 0; base < n; base += kChunk) {
+    if (base + kChunk < n) load(base + kChunk, next);
+    int run = 0;
 #pragma unroll
-    for (int j = 0; j < kItems; ++j) {
-      const int i = base + threadIdx.x * kItems + j;
-      if (i < n) first[i] = run;
-      run += v[j];
+    for (int j = 0; j < kRounds; ++j) {
+      const int inc = warp_inclusive_scan(v[j]);
+      const int excl = run + inc - v[j];
+      run += __shfl_sync(0xffffffffu, inc, 31);
+      v[j] = excl;  // exclusive prefix inside the warp's 512 counts
     }
+    if (lane == 0) warp_sums[warp] = run;
     __syncthreads();
-    if (threadIdx.x == 0) carry += total;
+    if (warp == 0) warp_sums[lane] = warp_inclusive_scan(warp_sums[lane]);
     __syncthreads();
+    const int offset = carry + (warp ? warp_sums[warp - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < kRounds; ++j) {
+      const int i = base + warp * (32 * kRounds) + j * 32 + lane;
+      if (i < n) first[i] = offset + v[j];
+    }
+    carry += warp_sums[31];  // the same in every thread
+    __syncthreads();          // warp_sums is rewritten by the next pass
+#pragma unroll
+    for (int j = 0; j < kRounds; ++j) v[j] = next[j];
   }
   if (threadIdx.x == 0) first[n] = carry;
 }
@@ -210,14 +236,38 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
 // box touches. Order inside a bin is irrelevant to the result.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B) {
   const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (g >= a.total_tris) return;
-  const int4 box = a.bbox[g];
-  if (box.y <= box.x) return;
-  int tx0, tx1, ty0, ty1;
-  tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
-  if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > a.large_tiles) return;
-  const int img = find_segment(B.tri_start, B.n, g);
-  const int base = B.tile_start[img], tx = B.tiles_x[img];
+  const int lane = threadIdx.x & 31;
+  // Every lane stays to the warp-wide match below; `binned` marks lanes
+  // with a triangle to bin.
+  bool binned = false;
+  int tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, base = 0, tx = 0;
+  if (g < a.total_tris) {
+    const int4 box = a.bbox[g];
+    if (box.y > box.x) {
+      tile_rect(box, a.TW, a.TH, tx0, tx1, ty0, ty1);
+      if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) <= a.large_tiles) {
+        binned = true;
+        const int img = find_segment(B.tri_start, B.n, g);
+        base = B.tile_start[img];
+        tx = B.tiles_x[img];
+      }
+    }
+  }
+  // Triangles inside one tile (most of them, and neighbours in the mesh
+  // order) take their bin slots with one atomic per tile per warp.
+  const bool single = binned && tx0 == tx1 && ty0 == ty1;
+  const int tile0 = base + ty0 * tx + tx0;
+  const unsigned group = __match_any_sync(0xffffffffu, single ? tile0 : -1 - lane);
+  const int leader = __ffs(group) - 1;
+  int slot = 0;
+  if (single && lane == leader) slot = atomicAdd(&a.tile_fill[tile0], __popc(group));
+  slot = __shfl_sync(0xffffffffu, slot, leader);
+  if (single) {
+    const int rank = __popc(group & ((1u << lane) - 1u));
+    a.bins[a.tile_first[tile0] + slot + rank] = int(g);
+    return;
+  }
+  if (!binned) return;
   for (int y = ty0; y <= ty1; ++y)
     for (int x = tx0; x <= tx1; ++x) {
       const int tile = base + y * tx + x;

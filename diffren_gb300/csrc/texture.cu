@@ -131,6 +131,84 @@ __global__ void __launch_bounds__(256) texture_fwd_kernel(TexArgs a) {
   }
 }
 
+// The common case on 32-bit texel indices: four channels, edge padding, a
+// texture of fewer than 2^29 texels, 8-byte aligned uv and 16-byte aligned
+// texture and output. Same operations and order as texture_fwd_kernel.
+__global__ void __launch_bounds__(256) texture_fwd4_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const float2 uv = __ldg(reinterpret_cast<const float2*>(a.uv) + i);
+  const bool texels = a.flags & DR_TEXTURE_TEXEL_UNITS;
+  const float qc = __fsub_rn(texels ? uv.x : __fmul_rn(uv.x, __int2float_rn(a.W)), 0.5f);
+  const float qr = __fsub_rn(texels ? uv.y : __fmul_rn(uv.y, __int2float_rn(a.H)), 0.5f);
+  const Axis r = axis_of(__fadd_rn(qr, 1.0f), a.H);
+  const Axis c = axis_of(__fadd_rn(qc, 1.0f), a.W);
+  // padded rows / columns f and f + 1 are texture rows f - 1 and f, clamped
+  const unsigned r0 = unsigned(max(r.f - 1, 0)) * unsigned(a.W);
+  const unsigned r1 = unsigned(min(r.f, a.H - 1)) * unsigned(a.W);
+  const unsigned c0 = unsigned(max(c.f - 1, 0)), c1 = unsigned(min(c.f, a.W - 1));
+  const float4* T = reinterpret_cast<const float4*>(a.tex);
+  const float4 t00 = __ldg(T + r0 + c0), t10 = __ldg(T + r1 + c0), t11 = __ldg(T + r1 + c1),
+               t01 = __ldg(T + r0 + c1);
+  const auto mix = [&](float x00, float x10, float x11, float x01) {
+    const float ll = __fmul_rn(__fmul_rn(x00, r.fw), c.fw);
+    const float ul = __fmul_rn(__fmul_rn(x10, r.cw), c.fw);
+    const float ur = __fmul_rn(__fmul_rn(x11, r.cw), c.cw);
+    const float lr = __fmul_rn(__fmul_rn(x01, r.fw), c.cw);
+    return __fadd_rn(__fadd_rn(__fadd_rn(ll, ul), ur), lr);
+  };
+  reinterpret_cast<float4*>(a.out)[i] =
+      make_float4(mix(t00.x, t10.x, t11.x, t01.x), mix(t00.y, t10.y, t11.y, t01.y),
+                  mix(t00.z, t10.z, t11.z, t01.z), mix(t00.w, t10.w, t11.w, t01.w));
+}
+
+// The VJP of texture_fwd4_kernel (same conditions; d_tex 16-byte aligned).
+__global__ void __launch_bounds__(256) texture_bwd4_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const float4 g = __ldg(reinterpret_cast<const float4*>(a.d_out) + i);
+  if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f && g.w == 0.0f) {
+    if (a.d_uv) reinterpret_cast<float2*>(a.d_uv)[i] = make_float2(0.0f, 0.0f);
+    return;
+  }
+  const float2 uv = __ldg(reinterpret_cast<const float2*>(a.uv) + i);
+  const bool texels = a.flags & DR_TEXTURE_TEXEL_UNITS;
+  const float qc = __fsub_rn(texels ? uv.x : __fmul_rn(uv.x, __int2float_rn(a.W)), 0.5f);
+  const float qr = __fsub_rn(texels ? uv.y : __fmul_rn(uv.y, __int2float_rn(a.H)), 0.5f);
+  const Axis r = axis_of(__fadd_rn(qr, 1.0f), a.H);
+  const Axis c = axis_of(__fadd_rn(qc, 1.0f), a.W);
+  const unsigned r0 = unsigned(max(r.f - 1, 0)) * unsigned(a.W);
+  const unsigned r1 = unsigned(min(r.f, a.H - 1)) * unsigned(a.W);
+  const unsigned c0 = unsigned(max(c.f - 1, 0)), c1 = unsigned(min(c.f, a.W - 1));
+  if (a.d_tex) {
+    float4* D = reinterpret_cast<float4*>(a.d_tex);
+    const auto add = [&](unsigned t, float w) {
+      atomicAdd(D + t, make_float4(g.x * w, g.y * w, g.z * w, g.w * w));
+    };
+    add(r0 + c0, r.fw * c.fw);
+    add(r1 + c0, r.cw * c.fw);
+    add(r1 + c1, r.cw * c.cw);
+    add(r0 + c1, r.fw * c.cw);
+  }
+  if (a.d_uv) {
+    const float4* T = reinterpret_cast<const float4*>(a.tex);
+    const float4 t00 = __ldg(T + r0 + c0), t10 = __ldg(T + r1 + c0), t11 = __ldg(T + r1 + c1),
+                 t01 = __ldg(T + r0 + c1);
+    float du = 0.0f, dv = 0.0f;
+    const auto step = [&](float gk, float d00, float d10, float d11, float d01) {
+      du += gk * (r.fw * (d01 - d00) + r.cw * (d11 - d10));
+      dv += gk * (c.fw * (d10 - d00) + c.cw * (d11 - d01));
+    };
+    step(g.x, t00.x, t10.x, t11.x, t01.x);
+    step(g.y, t00.y, t10.y, t11.y, t01.y);
+    step(g.z, t00.z, t10.z, t11.z, t01.z);
+    step(g.w, t00.w, t10.w, t11.w, t01.w);
+    reinterpret_cast<float2*>(a.d_uv)[i] =
+        make_float2(du * c.dcw * (texels ? 1.0f : __int2float_rn(a.W)),
+                    dv * r.dcw * (texels ? 1.0f : __int2float_rn(a.H)));
+  }
+}
+
 __global__ void __launch_bounds__(256) texture_bwd_kernel(TexArgs a) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -210,7 +288,14 @@ int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int 
   if (n == 0) return DR_OK;
   if (!out) { err = "out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
   TexArgs a{uv, tex, H, W, C, flags, n, out, nullptr, nullptr, nullptr};
-  texture_fwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  const bool fast = C == 4 && !(flags & DR_TEXTURE_PAD_ZERO) &&
+                    int64_t(H) * W < (int64_t(1) << 29) &&
+                    (reinterpret_cast<uintptr_t>(uv) & 7) == 0 &&
+                    ((reinterpret_cast<uintptr_t>(tex) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+  if (fast)
+    texture_fwd4_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  else
+    texture_fwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
   return launch_status("texture map", err);
 }
 
@@ -221,7 +306,15 @@ int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const flo
   if (n == 0) return DR_OK;
   if (!d_out) { err = "d_out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
   TexArgs a{uv, tex, H, W, C, flags, n, nullptr, d_out, d_uv, d_tex};
-  texture_bwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  const bool fast = C == 4 && !(flags & DR_TEXTURE_PAD_ZERO) &&
+                    int64_t(H) * W < (int64_t(1) << 29) &&
+                    ((reinterpret_cast<uintptr_t>(uv) | reinterpret_cast<uintptr_t>(d_uv)) & 7) == 0 &&
+                    ((reinterpret_cast<uintptr_t>(tex) | reinterpret_cast<uintptr_t>(d_out) |
+                      reinterpret_cast<uintptr_t>(d_tex)) & 15) == 0;
+  if (fast)
+    texture_bwd4_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+  else
+    texture_bwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
   return launch_status("texture map backward", err);
 }
 

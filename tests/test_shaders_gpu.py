@@ -20,7 +20,8 @@ def assert_grad_close(ours, ref):
   np.testing.assert_allclose(ours, ref, rtol=GRAD_RTOL, atol=GRAD_RTOL * scale)
 
 
-@pytest.mark.parametrize("shape", [(5, 7, 3), (16, 9, 4), (1, 1, 1), (33, 2, 2), (8, 8, 16)])
+@pytest.mark.parametrize("shape", [(5, 7, 3), (16, 9, 4), (1, 1, 4), (1, 1, 1), (33, 2, 2),
+                                   (8, 8, 16)])
 def test_texture_map_forward_matches_oracle(shape, device):
   rng = np.random.default_rng(sum(shape))
   tex = rng.uniform(-1, 1, shape).astype(np.float32)
@@ -57,12 +58,14 @@ def test_bilinear_resample_known_answers(device):
 
 
 @pytest.mark.parametrize("pad_mode", ["edge", "constant"])
-def test_texture_map_backward_matches_autograd(pad_mode, device):
+@pytest.mark.parametrize("channels", [3, 4])
+def test_texture_map_backward_matches_autograd(pad_mode, channels, device):
   rng = np.random.default_rng(11)
-  tex = rng.uniform(-1, 1, (6, 9, 3)).astype(np.float32)
+  tex = rng.uniform(-1, 1, (6, 9, channels)).astype(np.float32)
   loc = rng.uniform(-1.5, 10.5, (2000, 2)).astype(np.float32) * np.array([1.0, 6.0 / 9.0],
                                                                           np.float32)
-  g = rng.standard_normal((2000, 3)).astype(np.float32)
+  g = rng.standard_normal((2000, channels)).astype(np.float32)
+  g[::7] = 0.0  # points without gradient
   tl = torch.tensor(loc, dtype=torch.float64, requires_grad=True)
   tt = torch.tensor(tex, dtype=torch.float64, requires_grad=True)
   ref = texture.bilinear_resample_t(tt, tl, pad_mode)
@@ -87,3 +90,22 @@ def test_textured_square_golden(device):
   ok, msg = helpers.images_near_python(helpers.to_rgba(g["textured_square"]),
                                        helpers.pil_format(rendered.cpu().numpy()))
   assert ok, msg
+
+
+@pytest.mark.parametrize("channels", [2, 4])
+def test_texture_map_uv_backward_matches_autograd(channels, device):
+  """shaders.texture_map's VJP in uv units (edge clamping)."""
+  rng = np.random.default_rng(12)
+  tex = rng.uniform(0, 1, (7, 5, channels)).astype(np.float32)
+  uv = rng.uniform(-0.2, 1.2, (3000, 2)).astype(np.float32)
+  g = rng.standard_normal((3000, channels)).astype(np.float32)
+  tu = torch.tensor(uv, dtype=torch.float64, requires_grad=True)
+  tt = torch.tensor(tex, dtype=torch.float64, requires_grad=True)
+  ref = texture.texture_map_t(tu, tt)
+  gu, gt = torch.autograd.grad(ref, (tu, tt), torch.tensor(g, dtype=torch.float64))
+  du = torch.tensor(uv, device=device, requires_grad=True)
+  dt = torch.tensor(tex, device=device, requires_grad=True)
+  out = shaders.texture_map(du, dt)
+  ou, ot = torch.autograd.grad(out, (du, dt), torch.tensor(g, device=device))
+  assert_grad_close(ou.cpu().numpy(), gu.numpy())
+  assert_grad_close(ot.cpu().numpy(), gt.numpy())
