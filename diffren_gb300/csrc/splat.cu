@@ -601,21 +601,39 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
     const int64_t HW = int64_t(W) * H;
     const int64_t base = int64_t(L) * B.pix_off[tr.img];
     unsigned any = 0;
-    for (int i = threadIdx.x; i < kRR; i += blockDim.x) {
+    // Every depth of the thread's region samples is in flight at once; then
+    // only the positions and colors of foreground layers are read.
+    constexpr int kIt = (kRR + kTX * kTY - 1) / (kTX * kTY);
+    unsigned mk[kIt];
+#pragma unroll
+    for (int k = 0; k < kIt; ++k) {
+      const int i = threadIdx.x + k * kTX * kTY;
+      const int ry = i / kRS;
+      const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
+      const bool in = i < kRR && x >= 0 && y >= 0 && x < W && y < H;
+      const int64_t e0 = base + int64_t(y) * W + x;
+      mk[k] = 0;
+      if (in && a.zb)
+        for (int l = 0; l < L; ++l) mk[k] |= unsigned(__ldg(a.zb + e0 + l * HW) != 1.0f) << l;
+    }
+#pragma unroll
+    for (int k = 0; k < kIt; ++k) {
+      const int i = threadIdx.x + k * kTX * kTY;
+      if (i >= kRR) break;
+      unsigned m = mk[k];
       const int ry = i / kRS;
       const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
       const bool in = x >= 0 && y >= 0 && x < W && y < H;
       const int64_t e0 = base + int64_t(y) * W + x;
-      // With a depth buffer, its L independent 4-byte loads find the
-      // foreground layers first; only their positions are read.
-      unsigned m = 0;
-      if (in && a.zb)
-        for (int l = 0; l < L; ++l) m |= unsigned(__ldg(a.zb + e0 + l * HW) != 1.0f) << l;
       for (int l = 0; l < L; ++l) {
         float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-        if (in && (!a.zb || ((m >> l) & 1u))) q = __ldg(a.vp + e0 + l * HW);
+        const bool fgbit = in && ((m >> l) & 1u);
+        if (in && (!a.zb || fgbit)) q = __ldg(a.vp + e0 + l * HW);
+        float4 c[Q];
+        // with a depth buffer the color load need not wait for the position
+        if (a.zb && fgbit) load_groups<C>(a.colors + (e0 + l * HW) * C, c);
         zs[l * kRR + i] = q.z;
-        const float fgw = fg_weight(a.zb != nullptr, in && ((m >> l) & 1u), q);
+        const float fgw = fg_weight(a.zb != nullptr, fgbit, q);
         if (fgw != 0.0f) {
           m |= 1u << l;
           const Taps t = taps_of(q, fgw, a.coef);
@@ -624,8 +642,7 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
             wx[(l * 3 + u) * kRR + i] = t.ex[u];
             wy[(l * 3 + u) * kRR + i] = t.ey[u];
           }
-          float4 c[Q];
-          load_groups<C>(a.colors + (e0 + l * HW) * C, c);
+          if (!a.zb) load_groups<C>(a.colors + (e0 + l * HW) * C, c);
 #pragma unroll
           for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + i] = c[g];
         }
