@@ -131,6 +131,7 @@ int over_launch(OverArgs a, const dr_image_desc* images, int n, bool backward,
     return DR_ERR_INVALID_ARGUMENT;
   }
   if (a.C < 1) { err = "channels must be >= 1"; return DR_ERR_INVALID_ARGUMENT; }
+  // Every group is checked before the first launch.
   Batch b;
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE)
     if (!make_batch(images + g0, std::min(n - g0, DR_MAX_BATCH_INLINE), a.L, 16, 16, b, err))
