@@ -8,8 +8,9 @@ It (1) compiles the reference's own CPU rasterizer in place
 geometry (raster_ref.npz); (2) extracts the reference tests' fixtures and
 known answers from their source text (cube vertices, triangle cases, the
 differentiable-barycentrics Jacobian of rasterize_test.py:216-224); (3)
-decodes the small golden PNGs the GPU tests compare against. Nothing here is
-used at run time by the library.
+decodes the small golden PNGs the GPU tests compare against, and (4) keeps
+the textured spot mesh, its texture and its blurred target render
+(spot.npz). Nothing here is used at run time by the library.
 """
 import argparse
 import ast
@@ -203,6 +204,27 @@ def main():
                                                    "shaders_test.py")))
   imgs["sphere_disparity"] = png.read_png(os.path.join(data, "Sphere_Disparity.png"))
   np.savez_compressed(os.path.join(HERE, "render_goldens.npz"), **imgs)
+
+  # The textured spot of splat_test.py:227-277: the mesh flattened and scaled
+  # as test_utils.load_test_obj does (positions x 0.2), its texture, and the
+  # target image blurred as load_and_blur_image does (gaussian, sigma 0.5,
+  # edge mode 'nearest', truncated at 4 sigma, per channel), formatted like
+  # get_pil_formatted_image.
+  from scipy import ndimage
+  pos, uv, nrm, tri = helpers.load_obj_attributes(os.path.join(data, "spot_triangulated.obj"))
+  assert uv is not None and nrm is None
+  target = png.read_png(os.path.join(data, "Spot_Textured.png"))[..., :3].astype(np.float32)
+  blurred = ndimage.gaussian_filter(target / 255.0, sigma=(0.5, 0.5, 0.0), mode="nearest",
+                                    truncate=4.0)
+  np.savez_compressed(os.path.join(HERE, "spot.npz"), positions=pos * np.float32(0.2),
+                      uvs=uv, triangles=tri,
+                      texture=png.read_png(os.path.join(data, "spot_texture.png")),
+                      target=helpers.pil_format(blurred),
+                      # shaders_test.py:76-168: OVER renders of the same spot
+                      diffuse=png.read_png(os.path.join(data, "Spot_Textured.png")),
+                      point=png.read_png(os.path.join(data, "Spot_Textured_Pt_Light.png")),
+                      phong_point=png.read_png(
+                          os.path.join(data, "Spot_Textured_Phong_Point.png")))
 
   # Bilinear resampling known answers (image_test.py boundary cases).
   np.savez_compressed(os.path.join(HERE, "texture_cases.npz"),

@@ -28,6 +28,8 @@ def eye_position(view_name):
     return np.array((2.0, 3.0, 6.0)), np.array((0.0, 1.0, 0.0))
   if view_name.startswith("view_2"):
     return np.array((-3.0, 1.0, 6.0)), np.array((0.0, 1.0, 0.0))
+  if view_name.startswith("spot"):
+    return np.array((0.2, 0.3, -0.5)), np.array((0.0, -1.0, 0.0))
   raise ValueError(view_name)
 
 
@@ -169,6 +171,41 @@ def load_obj(path):
         tri.append(index[name])
       tris.append(tri)
   return np.array(flat, np.float32), np.array(tris, np.int32)
+
+
+def load_obj_attributes(path):
+  """Wavefront OBJ -> (positions [N,3], uvs [N,2] or None, normals [N,3] or
+  None, triangles [T,3]) flattened as diffren/common/obj_loader.py:24-104
+  does: one vertex per distinct face-vertex token ('v', 'v/vt', 'v//vn',
+  'v/vt/vn'), numbered in order of first appearance, zeros for an attribute
+  a token lacks, and each attribute kept only if some token uses it."""
+  lists = {"v": [], "vt": [], "vn": []}
+  flat, index, tris, used = [], {}, [], {"vt": False, "vn": False}
+  for line in open(path):
+    p = line.split()
+    if not p:
+      continue
+    if p[0] in lists:
+      lists[p[0]].append([float(x) for x in p[1:]])
+    elif p[0] == "f":
+      tri = []
+      for name in p[1:4]:
+        if name not in index:
+          parts = (name.split("/") + ["", ""])[:3]
+          row = list(lists["v"][int(parts[0]) - 1][:3])
+          for kind, idx, width in (("vt", parts[1], 2), ("vn", parts[2], 3)):
+            if idx:
+              row += lists[kind][int(idx) - 1][:width]
+              used[kind] = True
+            else:
+              row += [0.0] * width
+          index[name] = len(flat)
+          flat.append(row)
+        tri.append(index[name])
+      tris.append(tri)
+  a = np.array(flat, np.float32)
+  return (a[:, :3], a[:, 3:5] if used["vt"] else None, a[:, 5:8] if used["vn"] else None,
+          np.array(tris, np.int32))
 
 
 def homogeneous(v):

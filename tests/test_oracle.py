@@ -296,3 +296,66 @@ def test_vertex_normals_torch_oracle_matches_numpy_and_finite_differences():
   np.testing.assert_allclose(mesh.vertex_normals_t(tv, tt).detach().numpy(),
                              mesh.vertex_normals(v, t), rtol=1e-12, atol=1e-12)
   assert torch.autograd.gradcheck(lambda x: mesh.vertex_normals_t(x, tt), (tv,))
+
+
+def test_oracle_spot_textured_golden():
+  """splat_test.py:227-277 ('spot') through the CPU restatement: vertex
+  normals, texture map, diffuse light (shaders.py:68-97), splat; pins the
+  restated shading chain to the reference's blurred golden render."""
+  from oracle import mesh as omesh
+  from oracle import splat as np_splat
+  from oracle import texture
+  g = helpers.golden("spot.npz")
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("spot")
+  pos, tris, uvs = g["positions"], g["triangles"], g["uvs"]
+  clip = raster.transform(proj.astype(np.float32), pos)
+  ids, z, b = raster.rasterize(clip, tris, helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT, 1, 1)
+  normals = omesh.vertex_normals(pos, tris).astype(np.float32)
+  uv = np_splat.interpolate(uvs, ids, z, b, tris)
+  n = np_splat.interpolate(normals, ids, z, b, tris)
+  tex = np.flipud(g["texture"]).astype(np.float32) / np.float32(255.0)
+  rgb = texture.texture_map(uv.reshape(-1, 2), tex).reshape(uv.shape[:-1] + (3,))
+  d = np.array([0.5, 0.5, 1.0], np.float32)
+  d = d / np.sqrt((d * d).sum() + np.float32(1e-12))
+  ndl = np.clip((n * d).sum(-1, keepdims=True), 0.0, 1.0)
+  lit = rgb * np.float32(0.5) + rgb * np.float32(0.5) * ndl
+  rgba = np.concatenate([lit, (uv[..., :1] > -1.0).astype(np.float32)], -1).astype(np.float32)
+  out, _, _ = np_splat.splat_shaded_pixels(clip, ids, z, b, tris, rgba, helpers.IMAGE_WIDTH,
+                                           helpers.IMAGE_HEIGHT)
+  ok, msg = helpers.images_near_python(g["target"], helpers.pil_format(out[..., :3]))
+  assert ok, msg
+
+
+@pytest.mark.parametrize("lighting", ["diffuse", "point", "phong_point"])
+def test_oracle_spot_lighting_goldens(lighting):
+  """shaders_test.py:76-168 through the CPU restatement: the spot with
+  texture and diffuse / point / Blinn-Phong point lighting (shaders.py:68-173)
+  on vertex normals (mesh.py:22-52), CompositingMode.OVER, one layer."""
+  from oracle import mesh as omesh
+  from oracle import shading
+  from oracle import splat as np_splat
+  from oracle import texture
+  g = helpers.golden("spot.npz")
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("spot")
+  pos, tris, uvs = g["positions"], g["triangles"], g["uvs"]
+  clip = raster.transform(proj.astype(np.float32), pos)
+  ids, z, b = raster.rasterize(clip, tris, helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT, 1, 1)
+  normals = omesh.vertex_normals(pos, tris).astype(np.float32)
+  uv = np_splat.interpolate(uvs, ids, z, b, tris)
+  n = np_splat.interpolate(normals, ids, z, b, tris)
+  p = np_splat.interpolate(pos, ids, z, b, tris)
+  tex = np.flipud(g["texture"]).astype(np.float32) / np.float32(255.0)
+  rgb = texture.texture_map(uv.reshape(-1, 2), tex).reshape(uv.shape[:-1] + (3,))
+  eye = helpers.eye_position("spot")[0].astype(np.float32)
+  if lighting == "diffuse":
+    d = np.array([0.5, 0.5, 1.0], np.float32)
+    d = d / np.sqrt((d * d).sum() + np.float32(1e-12))
+    ndl = np.clip((n * d).sum(-1, keepdims=True), 0.0, 1.0)
+    lit = rgb * np.float32(0.5) + rgb * np.float32(0.5) * ndl
+  else:
+    kw = dict(eye=tuple(eye), ks=1.0, ns=50.0) if lighting == "phong_point" else {}
+    lit = shading.point_light(torch.tensor(rgb), torch.tensor(n), torch.tensor(p),
+                              tuple(eye), **kw).numpy()
+  out = (lit * (z != 1.0)[..., None])[0]  # OVER of one masked layer
+  ok, msg = helpers.images_near_python(g[lighting], helpers.pil_format(out))
+  assert ok, msg

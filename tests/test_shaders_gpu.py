@@ -109,3 +109,60 @@ def test_texture_map_uv_backward_matches_autograd(channels, device):
   ou, ot = torch.autograd.grad(out, (du, dt), torch.tensor(g, device=device))
   assert_grad_close(ou.cpu().numpy(), gu.numpy())
   assert_grad_close(ot.cpu().numpy(), gt.numpy())
+
+
+def test_spot_textured_golden(device):
+  """splat_test.py:227-277 ('spot'): the textured, diffusely lit spot with
+  normals from mesh.compute_vertex_normals, through render_triangles,
+  against the reference's blurred golden render."""
+  from diffren_gb300 import mesh
+  g = helpers.golden("spot.npz")
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("spot")
+  pos = torch.tensor(g["positions"], device=device)
+  tris = torch.tensor(g["triangles"], device=device)
+  # load_texture: float [0, 1], flipped to the lower-left origin.
+  tex = torch.tensor(np.flipud(g["texture"]).astype(np.float32) / 255.0, device=device)
+  attrs = {"uvs": torch.tensor(g["uvs"], device=device),
+           "normals": mesh.compute_vertex_normals(pos, tris)}
+
+  def shade(a):
+    lit = shaders.diffuse_light(shaders.texture_map(a["uvs"], tex), a["normals"])
+    alpha = (a["uvs"][..., 0:1] > -1.0).float()
+    return torch.cat([lit, alpha], -1)
+
+  rendered = render.render_triangles(pos, attrs, tris, torch.tensor(proj, dtype=torch.float32,
+                                                                    device=device),
+                                     helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT, shade)
+  ok, msg = helpers.images_near_python(g["target"],
+                                       helpers.pil_format(rendered[..., :3].cpu().numpy()))
+  assert ok, msg
+
+
+@pytest.mark.parametrize("lighting", ["diffuse", "point", "phong_point"])
+def test_spot_lighting_goldens(lighting, device):
+  """shaders_test.py:76-168: the spot with texture and diffuse / point /
+  Blinn-Phong point lighting on vertex normals, CompositingMode.OVER (the
+  OVER kernel), against the reference's golden renders."""
+  from diffren_gb300 import constants, mesh
+  g = helpers.golden("spot.npz")
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("spot")
+  pos = torch.tensor(g["positions"], device=device)
+  tris = torch.tensor(g["triangles"], device=device)
+  tex = torch.tensor(np.flipud(g["texture"]).astype(np.float32) / 255.0, device=device)
+  eye = tuple(float(x) for x in helpers.eye_position("spot")[0])
+  attrs = {"uvs": torch.tensor(g["uvs"], device=device), "positions": pos,
+           "normals": mesh.compute_vertex_normals(pos, tris)}
+
+  def shade(a):
+    textured = shaders.texture_map(a["uvs"], tex)
+    if lighting == "diffuse":
+      return shaders.diffuse_light(textured, a["normals"])
+    kw = dict(eye_position=eye, ks=1.0, ns=50.0) if lighting == "phong_point" else {}
+    return shaders.point_light(textured, a["normals"], a["positions"], eye, **kw)
+
+  rendered = render.render_triangles(pos, attrs, tris,
+                                     torch.tensor(proj, dtype=torch.float32, device=device),
+                                     helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT, shade,
+                                     compositing_mode=constants.CompositingMode.OVER)
+  ok, msg = helpers.images_near_python(g[lighting], helpers.pil_format(rendered.cpu().numpy()))
+  assert ok, msg
