@@ -14,6 +14,7 @@ DR_OK = 0
 DR_CULL_NONE, DR_CULL_BACK, DR_CULL_FRONT = 0, 1, 2
 DR_DEPTH_DISCRETIZED, DR_DEPTH_FLOAT = 0, 1
 DR_FLAG_INDEX_OUT_OF_RANGE = 1
+DR_FLAG_NONFINITE_VERTEX = 2
 DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8

@@ -142,6 +142,11 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
   } else {
     const float4* vb = a.verts + B.vertex_offset[img];
     const float4 v0 = vb[i0], v1 = vb[i1], v2 = vb[i2];
+    // x - x == 0 exactly for finite x, NaN for NaN and infinities.
+    const float probe = (v0.x - v0.x) + (v0.y - v0.y) + (v0.z - v0.z) + (v0.w - v0.w) +
+                        (v1.x - v1.x) + (v1.y - v1.y) + (v1.z - v1.z) + (v1.w - v1.w) +
+                        (v2.x - v2.x) + (v2.y - v2.y) + (v2.z - v2.z) + (v2.w - v2.w);
+    if (probe != 0.0f) atomicOr(&a.counters[1], DR_FLAG_NONFINITE_VERTEX);
     valid = triangle_box(v0, v1, v2, W, H, box);
     if (valid) {
       TriSetup s;

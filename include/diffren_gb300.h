@@ -82,6 +82,9 @@ extern "C" {
 /* Bits of the device error word (dr_read_error_flags). */
 #define DR_FLAG_INDEX_OUT_OF_RANGE 1u /* a triangle named a vertex >= V or < 0;
                                          that triangle was skipped */
+#define DR_FLAG_NONFINITE_VERTEX 2u   /* a triangle's clip vertex held a NaN or
+                                         infinity; it is rasterized as the
+                                         reference would (report only) */
 
 /* One image of a batch: its mesh and its resolution. */
 typedef struct dr_image_desc {

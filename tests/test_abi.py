@@ -122,11 +122,13 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
 def test_python_constants_match_header():
   with open(HEADER) as f:
     src = f.read()
-  for name in ("DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_MAX_IMAGE_DIM",
+  for name in ("DR_FLAG_INDEX_OUT_OF_RANGE", "DR_FLAG_NONFINITE_VERTEX", "DR_TEXTURE_PAD_ZERO",
+               "DR_TEXTURE_TEXEL_UNITS",
+               "DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_MAX_IMAGE_DIM",
                "DR_MAX_SPLAT_CHANNELS", "DR_OK",
                "DR_CULL_NONE", "DR_CULL_BACK", "DR_CULL_FRONT", "DR_DEPTH_DISCRETIZED",
                "DR_DEPTH_FLOAT"):
-    m = re.search(r"#define %s (\d+)" % name, src)
+    m = re.search(r"#define %s (\d+)u?" % name, src)
     assert m and int(m.group(1)) == getattr(_lib, name), name
   assert kernels._groups(kernels.ImageBatch([1] * 129, [1] * 129, [0] * 129,
                                             [0] * 129)) == 2

@@ -163,6 +163,26 @@ def test_out_of_range_indices_are_skipped_and_flagged(device):
   np.testing.assert_array_equal(ids.view(1, 32, 32).cpu().numpy(), ref[0])
 
 
+def test_nonfinite_vertices_are_flagged_and_rasterized_as_the_oracle(device):
+  v = np.array([[-0.5, -0.5, 0.5, 1], [0.5, -0.5, 0.5, 1], [0, 0.5, 0.5, 1],
+                [0.2, 0.2, np.nan, 1], [0.9, 0.1, 0.5, 1], [0.1, 0.9, 0.5, np.inf]], np.float32)
+  t = np.array([[0, 1, 2], [3, 4, 5], [0, 4, 2]], np.int32)
+  batch = kernels.ImageBatch.single(32, 32, 6, 3)
+  cfg = kernels.raster_config(2, 0, 0)
+  ws = kernels.Workspace(device)
+  ids, z, _ = kernels.rasterize_packed(torch.tensor(v, device=device),
+                                       torch.tensor(t, device=device), batch, cfg, workspace=ws)
+  assert kernels.read_error_flags(ws, device) & _lib.DR_FLAG_NONFINITE_VERTEX
+  ref = raster.rasterize(v, t, 32, 32, 2, 0)
+  np.testing.assert_array_equal(ids.view(2, 32, 32).cpu().numpy(), ref[0])
+  # finite input raises no flag
+  ws2 = kernels.Workspace(device)
+  kernels.rasterize_packed(torch.tensor(v[:3], device=device),
+                           torch.tensor(t[:1], device=device),
+                           kernels.ImageBatch.single(32, 32, 3, 1), cfg, workspace=ws2)
+  assert kernels.read_error_flags(ws2, device) == 0
+
+
 def test_invalid_arguments_raise(device):
   v = torch.zeros(3, 4, device=device)
   t = torch.zeros(1, 3, dtype=torch.int32, device=device)
