@@ -300,16 +300,19 @@ def run_ours(args, rank, world, device):
     cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
   cams_h = torch.from_numpy(np.stack(wl.cams)).pin_memory()
   target = torch.from_numpy(np.concatenate([t.reshape(-1, 4) for t in wl.targets])).to(device)
-  verts = verts_h.to(device)
-  cols = cols_h.to(device)
-  cams = cams_h.to(device)
-  g_v = torch.empty_like(verts)
-  g_c = torch.empty_like(cols)
-  loss_out = torch.empty((), device=device)
+  # Two sets of device inputs and outputs: the end-to-end loop below runs
+  # one step on each set in turn while the other set's copies are in flight.
+  sets = [dict(verts=verts_h.to(device), cols=cols_h.to(device), cams=cams_h.to(device))
+          for _ in range(2)]
+  for b in sets:
+    b.update(g_v=torch.empty_like(b["verts"]), g_c=torch.empty_like(b["cols"]),
+             loss=torch.empty((), device=device))
+  verts, cams = sets[0]["verts"], sets[0]["cams"]
 
-  def step():
-    v = verts.detach().requires_grad_(True)
-    c = cols.detach().requires_grad_(True)
+  def step(b=sets[0]):
+    v = b["verts"].detach().requires_grad_(True)
+    c = b["cols"].detach().requires_grad_(True)
+    cams = b["cams"]
     if textured:
       out = r.render(v, {"uv": uv}, cams, lambda a: shaders.texture_map(a["uv"], c))
     elif wl.lit:
@@ -319,9 +322,9 @@ def run_ours(args, rank, world, device):
       out = r.render(v, {"rgba": rgba(c)}, cams, shader)
     loss = l2_loss(out, target)
     gv, gc = torch.autograd.grad(loss, (v, c))
-    g_v.copy_(gv)
-    g_c.copy_(gc)
-    loss_out.copy_(loss.detach())
+    b["g_v"].copy_(gv)
+    b["g_c"].copy_(gc)
+    b["loss"].copy_(loss.detach())
 
   # Eager warm-up on a side stream, then capture the step.
   s = torch.cuda.Stream(device)
@@ -347,7 +350,14 @@ def run_ours(args, rank, world, device):
   del z_fg
   graph = torch.cuda.CUDAGraph()
   with torch.cuda.graph(graph):
-    step()
+    step(sets[0])
+  # The same step on the second buffer set, sharing the first graph's
+  # memory pool (the two graphs only ever replay one after the other on
+  # one stream).
+  graph_b = torch.cuda.CUDAGraph()
+  with torch.cuda.graph(graph_b, pool=graph.pool()):
+    step(sets[1])
+  graphs = (graph, graph_b)
   for _ in range(args.warmup):
     graph.replay()
   torch.cuda.synchronize(device)
@@ -371,54 +381,52 @@ def run_ours(args, rank, world, device):
     ms = timed(graph.replay, args.steps)
     time.sleep(0.25)  # let the sample that covers the region's end arrive
   clock = clocks.summary(start)
-  loss_val = float(loss_out)
+  loss_val = float(sets[0]["loss"])
 
   # e2e: public API with host buffers. Every step copies its inputs from
-  # pinned host memory and its loss and gradients back. The copies run on
-  # two copy streams through staging buffers in HBM, so that step i+1's
-  # inputs arrive and step i-1's gradients leave while step i computes; the
-  # timed region runs from before the first input copy to the end of the
-  # last gradient copy.
+  # pinned host memory and its loss and gradients back. Steps alternate
+  # between the two buffer sets (and their graphs), so that step i+1's
+  # inputs arrive and step i's gradients leave on two copy streams while
+  # the next step computes; the timed region runs from before the first
+  # input copy to the end of the last gradient copy.
   gv_h = torch.empty_like(verts_h).pin_memory()
   gc_h = torch.empty_like(cols_h).pin_memory()
   loss_h = torch.empty((), pin_memory=True)
   h2d_s = torch.cuda.Stream(device)
   d2h_s = torch.cuda.Stream(device)
-  stage_in = [torch.empty_like(x) for x in (verts, cols, cams)]
-  stage_out = [torch.empty_like(x) for x in (g_v, g_c, loss_out)]
 
   def e2e_steps(k):
     cur = torch.cuda.current_stream(device)
-    in_ready, in_free = torch.cuda.Event(), torch.cuda.Event()
-    out_ready, out_free = torch.cuda.Event(), torch.cuda.Event()
+    in_ready = [torch.cuda.Event(), torch.cuda.Event()]
+    done = [torch.cuda.Event(), torch.cuda.Event()]
+    out_free = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def upload():
+    def upload(j):
       with torch.cuda.stream(h2d_s):
-        for dst, src in zip(stage_in, (verts_h, cols_h, cams_h)):
-          dst.copy_(src, non_blocking=True)
-        in_ready.record(h2d_s)
+        b = sets[j]
+        for name, src in (("verts", verts_h), ("cols", cols_h), ("cams", cams_h)):
+          b[name].copy_(src, non_blocking=True)
+        in_ready[j].record(h2d_s)
 
     h2d_s.wait_stream(cur)
-    upload()
+    upload(0)
     for i in range(k):
-      cur.wait_event(in_ready)
-      for dst, src in zip((verts, cols, cams), stage_in):
-        dst.copy_(src)
-      in_free.record(cur)
+      j = i % 2
+      cur.wait_event(in_ready[j])
+      if i >= 2:
+        cur.wait_event(out_free[j])  # step i-2's gradients have left set j
+      graphs[j].replay()
+      done[j].record(cur)
       if i + 1 < k:
-        h2d_s.wait_event(in_free)
-        upload()
-      graph.replay()
-      if i > 0:
-        cur.wait_event(out_free)
-      for dst, src in zip(stage_out, (g_v, g_c, loss_out)):
-        dst.copy_(src)
-      out_ready.record(cur)
-      d2h_s.wait_event(out_ready)
+        if i >= 1:
+          h2d_s.wait_event(done[1 - j])  # step i-1 has finished with set 1-j
+        upload(1 - j)
+      d2h_s.wait_event(done[j])
       with torch.cuda.stream(d2h_s):
-        for dst, src in zip((gv_h, gc_h, loss_h), stage_out):
-          dst.copy_(src, non_blocking=True)
-        out_free.record(d2h_s)
+        b = sets[j]
+        for dst, name in ((gv_h, "g_v"), (gc_h, "g_c"), (loss_h, "loss")):
+          dst.copy_(b[name], non_blocking=True)
+        out_free[j].record(d2h_s)
     cur.wait_stream(d2h_s)
 
   e2e_steps(2)
