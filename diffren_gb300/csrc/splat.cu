@@ -225,7 +225,7 @@ __device__ __forceinline__ float4 run_sum4(float4 v, int lane, int last) {
 }
 
 constexpr int kMaxRuns = 4;  // sum runs when a warp has at most this many
-constexpr int kVjpThreads = 256;
+constexpr int kVjpThreads = 512;
 constexpr int kVjpPerThread = 8;  // samples whose depth each thread tests
 constexpr int kVjpBlock = kVjpThreads * kVjpPerThread;
 
