@@ -379,6 +379,7 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_warp[kThreads / 32];
   __shared__ int s_item;
+  __shared__ int s_nfg;
   const int TW = a.TW, TH = a.TH, TP = TW * TH, L = LT > 0 ? LT : a.L;
   FineSmem s;
   {
@@ -525,39 +526,70 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
     // each layer sample's splat position and interpolated attributes.
     const int64_t HW = int64_t(H) * W;
     const int64_t base = int64_t(L) * B.pix_off[img];
-    for (int p = threadIdx.x; p < TP; p += kThreads) {
-      const int lx = p % TW, ly = p / TW;
-      if (lx >= tw || ly >= th) continue;
-      const int64_t pix = int64_t(y0 + ly) * W + (x0 + lx);
-      for (int l = 0; l < L; ++l) {
-        const unsigned long long key = s.keys[l * TP + p];
+    if constexpr (LT > 0) {
+      // Pass 1 writes background samples and lists the occupied slots
+      // (layer * TP + pixel, in the chunk arrays' space, dead by now); pass
+      // 2 runs the occupied slots with full warps.
+      unsigned short* list = reinterpret_cast<unsigned short*>(s.m);
+      if (threadIdx.x == 0) s_nfg = 0;
+      __syncthreads();
+      const int lane = threadIdx.x & 31;
+      for (int p0 = 0; p0 < TP; p0 += kThreads) {
+        const int p = p0 + threadIdx.x;
+        const int lx = p % TW, ly = p / TW;
+        const bool valid = p < TP && lx < tw && ly < th;
+        const int64_t pix = int64_t(y0 + ly) * W + (x0 + lx);
+#pragma unroll
+        for (int l = 0; l < LT; ++l) {
+          const unsigned long long key = valid ? s.keys[l * TP + p] : kEmpty;
+          const bool full = valid && key != kEmpty;
+          const unsigned ball = __ballot_sync(0xffffffffu, full);
+          int slot0 = 0;
+          if (lane == 0 && ball) slot0 = atomicAdd(&s_nfg, __popc(ball));
+          slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+          if (full) {
+            list[slot0 + __popc(ball & ((1u << lane) - 1u))] = (unsigned short)(l * TP + p);
+          } else if (valid) {
+            const int64_t o = base + l * HW + pix;
+            const float b0[3] = {0.0f, 0.0f, 0.0f};
+            a.ids[o] = disc ? 0 : -1;
+            a.z[o] = 1.0f;
+            float* bo = a.bary + 3 * o;
+            bo[0] = 0.0f;
+            bo[1] = 0.0f;
+            bo[2] = 0.0f;
+            if (kFused) write_sample(a, B, img, nullptr, 1.0f, b0, o);
+          }
+        }
+      }
+      __syncthreads();
+      const int nfg = s_nfg;
+      for (int f = threadIdx.x; f < nfg; f += kThreads) {
+        const int q = list[f];
+        const int l = q / TP, p = q - l * TP;
+        const int lx = p % TW, ly = p / TW;
+        const int64_t pix = int64_t(y0 + ly) * W + (x0 + lx);
+        const unsigned long long key = s.keys[q];
         const int64_t o = base + l * HW + pix;
         float b[3] = {0.0f, 0.0f, 0.0f};
-        int id;
-        float zz;
-        const TriSetup* st = nullptr;
-        if (key == kEmpty) {
-          id = disc ? 0 : -1;
-          zz = 1.0f;
-        } else {
-          id = int(uint32_t(key));
-          st = a.setup + tri0 + id;
-          long long m[9];
+        const int id = int(uint32_t(key));
+        const TriSetup* st = a.setup + tri0 + id;
+        long long m[9];
 #pragma unroll
-          for (int q = 0; q < 9; ++q) m[q] = __ldg(&st->m[q]);
-          long long e[3];
-          edge_values(m, s.pxf[lx], s.pyf[ly], e);
-          float bb[3];
-          barycentrics_of(e, bb);
-          if (disc) {
-            zz = undiscretize_z(uint32_t(key >> 32));
-          } else {
-            const float3 vz = make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
-            const float3 vw = make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
-            zz = fragment_z(bb, vz, vw);
-          }
-          if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
+        for (int k = 0; k < 9; ++k) m[k] = __ldg(&st->m[k]);
+        long long e[3];
+        edge_values(m, s.pxf[lx], s.pyf[ly], e);
+        float bb[3];
+        barycentrics_of(e, bb);
+        float zz;
+        if (disc) {
+          zz = undiscretize_z(uint32_t(key >> 32));
+        } else {
+          const float3 vz = make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
+          const float3 vw = make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
+          zz = fragment_z(bb, vz, vw);
         }
+        if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
         a.ids[o] = id;
         a.z[o] = zz;
         float* bo = a.bary + 3 * o;
@@ -566,8 +598,55 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
         bo[2] = b[2];
         if (kFused) write_sample(a, B, img, st, zz, b, o);
       }
+      __syncthreads();
+    } else {
+      // Any layer count: one pass, pixel by pixel.
+      for (int p = threadIdx.x; p < TP; p += kThreads) {
+        const int lx = p % TW, ly = p / TW;
+        if (lx >= tw || ly >= th) continue;
+        const int64_t pix = int64_t(y0 + ly) * W + (x0 + lx);
+        for (int l = 0; l < L; ++l) {
+          const unsigned long long key = s.keys[l * TP + p];
+          const int64_t o = base + l * HW + pix;
+          float b[3] = {0.0f, 0.0f, 0.0f};
+          int id;
+          float zz;
+          const TriSetup* st = nullptr;
+          if (key == kEmpty) {
+            id = disc ? 0 : -1;
+            zz = 1.0f;
+          } else {
+            id = int(uint32_t(key));
+            st = a.setup + tri0 + id;
+            long long m[9];
+  #pragma unroll
+            for (int q = 0; q < 9; ++q) m[q] = __ldg(&st->m[q]);
+            long long e[3];
+            edge_values(m, s.pxf[lx], s.pyf[ly], e);
+            float bb[3];
+            barycentrics_of(e, bb);
+            if (disc) {
+              zz = undiscretize_z(uint32_t(key >> 32));
+            } else {
+              const float3 vz =
+                  make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
+              const float3 vw =
+                  make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
+              zz = fragment_z(bb, vz, vw);
+            }
+            if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
+          }
+          a.ids[o] = id;
+          a.z[o] = zz;
+          float* bo = a.bary + 3 * o;
+          bo[0] = b[0];
+          bo[1] = b[1];
+          bo[2] = b[2];
+          if (kFused) write_sample(a, B, img, st, zz, b, o);
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
