@@ -616,6 +616,59 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
       if (in && a.zb)
         for (int l = 0; l < L; ++l) mk[k] |= unsigned(__ldg(a.zb + e0 + l * HW) != 1.0f) << l;
     }
+    if (LT > 0 && a.zb) {
+      // The warp's foreground (sample, layer) pairs are spread over its
+      // lanes: lane t takes the t-th set bit of the per-layer ballots, so
+      // the position and color loads and the tap weights run on full warps.
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int k = 0; k < kIt; ++k) {
+        const int i = threadIdx.x + k * kTX * kTY;
+        const bool valid = i < kRR;
+        const unsigned m = valid ? mk[k] : 0u;
+        if (valid) {
+          for (int l = 0; l < L; ++l)
+            if (!((m >> l) & 1u)) zs[l * kRR + i] = 1.0f;
+          fgm8[i] = (unsigned char)m;
+        }
+        any |= m;
+        unsigned masks[LT > 0 ? LT : 1];
+        int total = 0;
+#pragma unroll
+        for (int l = 0; l < (LT > 0 ? LT : 1); ++l) {
+          masks[l] = __ballot_sync(0xffffffffu, (m >> l) & 1u);
+          total += __popc(masks[l]);
+        }
+        const int wbase = (threadIdx.x & ~31) + k * kTX * kTY;
+        for (int t = lane; t < total; t += 32) {
+          int l = 0, r = t;
+#pragma unroll
+          for (int ll = 0; ll < (LT > 0 ? LT : 1) - 1; ++ll)
+            if (l == ll && r >= __popc(masks[ll])) { r -= __popc(masks[ll]); l = ll + 1; }
+          unsigned ml = masks[0];
+#pragma unroll
+          for (int ll = 1; ll < (LT > 0 ? LT : 1); ++ll)
+            if (l == ll) ml = masks[ll];
+          const int src = __fns(ml, 0, r + 1);
+          const int ii = wbase + src;
+          const int ry = ii / kRS;
+          const int x = tr.x0 - 1 + (ii - ry * kRS), y = tr.y0 - 1 + ry;
+          const int64_t e = base + int64_t(y) * W + x + l * HW;
+          const float4 q = __ldg(a.vp + e);
+          float4 c[Q];
+          load_groups<C>(a.colors + e * C, c);
+          zs[l * kRR + ii] = q.z;
+          const Taps tp = taps_of(q, 1.0f, a.coef);
+#pragma unroll
+          for (int u = 0; u < 3; ++u) {
+            wx[(l * 3 + u) * kRR + ii] = tp.ex[u];
+            wy[(l * 3 + u) * kRR + ii] = tp.ey[u];
+          }
+#pragma unroll
+          for (int g = 0; g < Q; ++g) col[(l * Q + g) * kRR + ii] = c[g];
+        }
+      }
+    } else
 #pragma unroll
     for (int k = 0; k < kIt; ++k) {
       const int i = threadIdx.x + k * kTX * kTY;
@@ -804,6 +857,41 @@ __device__ __forceinline__ void accum_adjoint(const float acc[3][C], const float
   }
 }
 
+// d color (dcol, float2 pairs) and d viewport xy of one foreground sample
+// from the adjoints of the 9 pixels it reached: tap (u, v) with weight
+// ex[u+1] ey[v+1] lands at ring pixel s1 + (u, v) in the class its surface
+// index picks.
+template <int Q>
+__device__ __forceinline__ void sample_adjoint(const Taps& tp, const float4* col,
+                                               const int (&surf)[9], unsigned ok, int l,
+                                               int s1, const float4* gs, const float* hs,
+                                               float2 (&dcol)[2 * Q], float& dvx,
+                                               float& dvy) {
+#pragma unroll
+  for (int j = 0; j < 9; ++j) {
+    if (!((ok >> j) & 1)) continue;
+    const int u = j / 3 - 1, v = j % 3 - 1;
+    const float w = __fmul_rn(tp.ex[u + 1], tp.ey[v + 1]);
+    const int k = surf[j] > l ? 0 : (surf[j] == l ? 1 : 2);
+    const int at = s1 + v * kRS + u;
+    const float4* gk = gs + k * Q * kRR + at;
+    float dw = hs[k * kRR + at];
+    const float2 w2 = make_float2(w, w);
+#pragma unroll
+    for (int g = 0; g < Q; ++g) {
+      const float4 gv = gk[g * kRR];
+      dcol[2 * g] = __ffma2_rn(w2, make_float2(gv.x, gv.y), dcol[2 * g]);
+      dcol[2 * g + 1] = __ffma2_rn(w2, make_float2(gv.z, gv.w), dcol[2 * g + 1]);
+      dw = fmaf(gv.x, col[g].x, fmaf(gv.y, col[g].y,
+                fmaf(gv.z, col[g].z, fmaf(gv.w, col[g].w, dw))));
+    }
+    // d w / d (x, y) = 4 w (dx, dy): the floor carries no gradient.
+    const float f = 4.0f * w * dw;
+    dvx = fmaf(f, tp.d0 + float(u), dvx);
+    dvy = fmaf(f, tp.d1 + float(v), dvy);
+  }
+}
+
 // Backward, gather form: the adjoints of the saved accumulators of the tile
 // plus a 1-pixel ring go to shared memory, g[k][q][i] (float4 groups of the
 // color adjoint of class k) and h[k][i] (weight adjoint), next to every
@@ -896,6 +984,81 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
     }
   }
   __syncthreads();
+  if (LT > 0 && a.zb) {
+    // Surface indexes of this thread's sample at the 9 pixels it reaches,
+    // then the warp's foreground (sample, layer) pairs spread over its lanes
+    // (lane t takes the t-th set bit of the per-layer ballots and the
+    // sample's surface indexes by shuffle); background pairs get zeros from
+    // their own thread.
+    const int lane = threadIdx.x & 31;
+    const int s1 = (ty + 1) * kRS + tx + 1;
+    int surf[9];
+    unsigned ok = 0;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const int u = j / 3 - 1, v = j % 3 - 1;
+      const int px = sx + u, py = sy + v;
+      const bool in = mine && px >= 0 && py >= 0 && px < W && py < H;
+      ok |= unsigned(in) << j;
+      surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
+    }
+    constexpr int kL = LT > 0 ? LT : 1;
+    unsigned masks[kL];
+    int total = 0;
+#pragma unroll
+    for (int l = 0; l < kL; ++l) {
+      const bool fg = mine && ((own >> l) & 1u);
+      if (mine && !fg) {
+        float dz[4 * Q];
+#pragma unroll
+        for (int c = 0; c < 4 * Q; ++c) dz[c] = 0.0f;
+        store_row<C>(a.d_colors + (ebase + l * HW) * C, dz);
+      }
+      masks[l] = __ballot_sync(0xffffffffu, fg);
+      total += __popc(masks[l]);
+    }
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      const bool active = t < total;
+      int l = 0, src = lane;
+      if (active) {
+        int r = t;
+#pragma unroll
+        for (int ll = 0; ll < kL - 1; ++ll)
+          if (l == ll && r >= __popc(masks[ll])) { r -= __popc(masks[ll]); l = ll + 1; }
+        unsigned ml = masks[0];
+#pragma unroll
+        for (int ll = 1; ll < kL; ++ll)
+          if (l == ll) ml = masks[ll];
+        src = __fns(ml, 0, r + 1);
+      }
+      int ss[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) ss[j] = __shfl_sync(0xffffffffu, surf[j], src);
+      const unsigned okv = __shfl_sync(0xffffffffu, ok, src);
+      if (!active) continue;
+      const int64_t e = lbase + int64_t(sy) * W + (tr.x0 + src) + l * HW;
+      const int s1s = (ty + 1) * kRS + src + 1;
+      const float4 q = __ldg(a.vp + e);
+      float2 dcol[2 * Q];
+#pragma unroll
+      for (int hh = 0; hh < 2 * Q; ++hh) dcol[hh] = make_float2(0.0f, 0.0f);
+      float dvx = 0.0f, dvy = 0.0f;
+      const Taps tp = taps_of(q, 1.0f, a.coef);
+      float4 col[Q];
+      load_groups<C>(a.colors + e * C, col);
+      sample_adjoint<Q>(tp, col, ss, okv, l, s1s, gs, hs, dcol, dvx, dvy);
+      float dc[4 * Q];
+#pragma unroll
+      for (int hh = 0; hh < 2 * Q; ++hh) {
+        dc[2 * hh] = dcol[hh].x;
+        dc[2 * hh + 1] = dcol[hh].y;
+      }
+      store_row<C>(a.d_colors + e * C, dc);
+      a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
+    }
+    return;
+  }
   if (!mine) return;
   const int s1 = (ty + 1) * kRS + tx + 1;  // this sample's pixel in the ring grid
   // Surface index of this sample's splat at each of the 9 pixels it reaches:
@@ -922,29 +1085,7 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
       const Taps t = taps_of(q, fgw, a.coef);
       float4 col[Q];
       load_groups<C>(a.colors + e * C, col);
-#pragma unroll
-      for (int j = 0; j < 9; ++j) {
-        if (!((ok >> j) & 1)) continue;
-        const int u = j / 3 - 1, v = j % 3 - 1;
-        const float w = __fmul_rn(t.ex[u + 1], t.ey[v + 1]);
-        const int k = surf[j] > l ? 0 : (surf[j] == l ? 1 : 2);
-        const int at = s1 + v * kRS + u;
-        const float4* gk = gs + k * Q * kRR + at;
-        float dw = hs[k * kRR + at];
-        const float2 w2 = make_float2(w, w);
-#pragma unroll
-        for (int g = 0; g < Q; ++g) {
-          const float4 gv = gk[g * kRR];
-          dcol[2 * g] = __ffma2_rn(w2, make_float2(gv.x, gv.y), dcol[2 * g]);
-          dcol[2 * g + 1] = __ffma2_rn(w2, make_float2(gv.z, gv.w), dcol[2 * g + 1]);
-          dw = fmaf(gv.x, col[g].x, fmaf(gv.y, col[g].y,
-                    fmaf(gv.z, col[g].z, fmaf(gv.w, col[g].w, dw))));
-        }
-        // d w / d (x, y) = 4 w (dx, dy): the floor carries no gradient.
-        const float f = 4.0f * w * dw;
-        dvx = fmaf(f, t.d0 + float(u), dvx);
-        dvy = fmaf(f, t.d1 + float(v), dvy);
-      }
+      sample_adjoint<Q>(t, col, surf, ok, l, s1, gs, hs, dcol, dvx, dvy);
     }
     float dc[4 * Q];
 #pragma unroll
