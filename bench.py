@@ -262,8 +262,8 @@ class ClockSampler:
 # (profiles/*_ragged8_subset.md): setup + tile scan + binning + fine raster;
 # splat forward; splat backward; samples VJP. Traffic grows with the layer
 # samples, so the full workload's traffic is this times its samples.
-TRAFFIC_PER_SAMPLE = {"raster": 44.2, "splat_fwd": 24.52, "splat_bwd": 43.29,
-                      "samples_bwd": 23.16}
+TRAFFIC_PER_SAMPLE = {"raster": 44.3, "splat_fwd": 24.48, "splat_bwd": 43.46,
+                      "samples_bwd": 23.15}
 
 
 def kernel_bytes(wl, fg, near=None, C=4, K=4):
