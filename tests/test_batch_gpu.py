@@ -192,3 +192,41 @@ def test_autotuned_renderer_matches_default(device, tmp_path, monkeypatch):
   r2.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
   assert (r2.config.tile_width, r2.config.tile_height, r2.config.large_tiles) == chosen
   autotune.clear_memory()
+
+
+@pytest.mark.parametrize("mode", [constants.CompositingMode.OVER, constants.CompositingMode.NONE])
+def test_batch_renderer_over_and_none_match_per_image(mode, device):
+  """BatchRenderer's OVER (the OVER kernel over the ragged batch) and NONE
+  modes equal each image's own render_triangles call, forward and backward."""
+  meshes, cams, sizes = ragged_scene(seed=4)
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=3, device=device,
+                              face_culling_mode=constants.FaceCullingMode.NONE)
+  c = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device,
+                   requires_grad=True)
+  v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device)
+  cam = torch.tensor(np.stack(cams), device=device)
+
+  def shade(a):  # semi-transparent, so that OVER mixes the layers
+    return a["rgba"] * 0.6
+
+  out = r.render(v, {"rgba": rgba(c)}, cam, shade, compositing_mode=mode)
+  g = torch.tensor(np.random.default_rng(1).standard_normal(tuple(out.shape)).astype(np.float32),
+                   device=device)
+  (gc,) = torch.autograd.grad(out, c, g)
+  coff = np.cumsum([0] + [len(m.vertices) for m in meshes])
+  poff = np.cumsum([0] + [w * h * (3 if mode == constants.CompositingMode.NONE else 1)
+                          for w, h in sizes])
+  for i, (m, cm, (w, h)) in enumerate(zip(meshes, cams, sizes)):
+    ci = torch.tensor(m.colors, device=device, requires_grad=True)
+    oi = render.render_triangles(torch.tensor(m.vertices, device=device), {"rgba": rgba(ci)},
+                                 torch.tensor(m.triangles, device=device),
+                                 torch.tensor(cm, device=device), w, h, shade, num_layers=3,
+                                 face_culling_mode=constants.FaceCullingMode.NONE,
+                                 compositing_mode=mode)
+    mine = out[int(poff[i]):int(poff[i + 1])].reshape(oi.shape)
+    assert torch.equal(mine, oi)
+    (gci,) = torch.autograd.grad(oi, ci, g[int(poff[i]):int(poff[i + 1])].reshape(oi.shape))
+    sl = slice(int(coff[i]), int(coff[i + 1]))
+    scale = float(gci.abs().max()) or 1.0
+    torch.testing.assert_close(gc[sl], gci, rtol=1e-4, atol=1e-5 * scale)
