@@ -344,4 +344,15 @@ int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buff
                 err);
 }
 
+int dr_splat_jvp(const float* positions, const float* z_buffer, const float* colors,
+                 const float* d_positions, const float* d_colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* d_image, void* stream) {
+  std::string err;
+  return finish(dr::splat_jvp_launch(positions, z_buffer, colors, d_positions, d_colors,
+                                     num_channels, images, num_images, num_layers, d_image,
+                                     as_stream(stream), err),
+                err);
+}
+
 }  // extern "C"

@@ -148,6 +148,10 @@ int positions_bwd_launch(const float* d_positions, const float* clip, const int3
 int splat_fwd_launch(const float* positions, const float* z_buffer, const float* colors, int C,
                      const dr_image_desc* images, int n, int L, float* out, float* saved,
                      float* accum, float* normalized, cudaStream_t stream, std::string& err);
+int splat_jvp_launch(const float* positions, const float* z_buffer, const float* colors,
+                     const float* d_positions, const float* d_colors, int C,
+                     const dr_image_desc* images, int n, int L, float* d_image,
+                     cudaStream_t stream, std::string& err);
 int splat_bwd_launch(const float* d_out, const float* positions, const float* z_buffer,
                      const float* colors, const float* saved, int C,
                      const dr_image_desc* images, int n, int L, float* d_colors,

@@ -1098,6 +1098,141 @@ __global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B)
   }
 }
 
+
+// Forward-mode derivative (JVP) of splat + normalize + over for tangents of
+// the sample positions (x, y) and, optionally, of the colors, with the
+// discrete state (floors, surface classes, foreground) held fixed, as
+// jax.jvp through splat.py:26-175 and composite.py:20-37 gives. A tap's
+// weight w = ex ey moves by d w = 4 w (dx tx + dy ty) for the sample's
+// position tangent (tx, ty) (dx, dy its tap offsets); each pixel carries the
+// accumulators and their tangents through the normalization (lax.max's
+// 0.5 tie rule) and the over compositing. Same tiling as the forward, one
+// pixel per thread; used by the forward-mode API, not on the benchmark path.
+template <int C>
+__global__ void __launch_bounds__(256) splat_jvp_kernel(SplatArgs a, const float4* d_vp,
+                                                       const float* d_colors, float* d_image,
+                                                       Batch B) {
+  constexpr int Q = Groups<C>::Q;
+  extern __shared__ __align__(16) float smem[];
+  const TileRef tr = tile_of(B);
+  const int L = a.L;
+  const int W = B.width[tr.img], H = B.height[tr.img];
+  float* zs = smem;                                         // [L][kRR]
+  float* wx = zs + L * kRR;                                 // [L][3][kRR]
+  float* wy = wx + 3 * L * kRR;                             // [L][3][kRR]
+  float4* tg = reinterpret_cast<float4*>(wy + 3 * L * kRR);  // [L][kRR] (d0, d1, tx, ty)
+  float4* col = tg + L * kRR;                               // [L][Q][kRR]
+  float4* dcol = col + Q * L * kRR;                         // [L][Q][kRR]
+  unsigned short* fgm = reinterpret_cast<unsigned short*>(dcol + Q * L * kRR);
+  const int64_t HW = int64_t(W) * H;
+  const int64_t base = int64_t(L) * B.pix_off[tr.img];
+  for (int i = threadIdx.x; i < kRR; i += blockDim.x) {
+    const int ry = i / kRS;
+    const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
+    const bool in = x >= 0 && y >= 0 && x < W && y < H;
+    const int64_t e0 = base + int64_t(y) * W + x;
+    unsigned m = 0;
+    for (int l = 0; l < L; ++l) {
+      const int64_t e = e0 + l * HW;
+      const bool fgbit = in && (a.zb ? __ldg(a.zb + e) != 1.0f : true);
+      float4 q = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+      if (fgbit) q = __ldg(a.vp + e);
+      zs[l * kRR + i] = q.z;
+      const float fgw = fg_weight(a.zb != nullptr, fgbit, q);
+      if (fgw != 0.0f) {
+        m |= 1u << l;
+        const Taps t = taps_of(q, fgw, a.coef);
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+          wx[(l * 3 + u) * kRR + i] = t.ex[u];
+          wy[(l * 3 + u) * kRR + i] = t.ey[u];
+        }
+        const float4 dq = d_vp ? __ldg(d_vp + e) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        tg[l * kRR + i] = make_float4(t.d0, t.d1, dq.x, dq.y);
+        float4 c[Q], dc[Q];
+        load_groups<C>(a.colors + e * C, c);
+        if (d_colors) {
+          load_groups<C>(d_colors + e * C, dc);
+        } else {
+#pragma unroll
+          for (int g = 0; g < Q; ++g) dc[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int g = 0; g < Q; ++g) {
+          col[(l * Q + g) * kRR + i] = c[g];
+          dcol[(l * Q + g) * kRR + i] = dc[g];
+        }
+      }
+    }
+    fgm[i] = (unsigned short)m;
+  }
+  __syncthreads();
+
+  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+  const int px = tr.x0 + tx, py = tr.y0 + ty;
+  if (px >= W || py >= H) return;
+  const int p = (ty + 1) * kRS + tx + 1;
+  float acc[3][4 * Q], dacc[3][4 * Q], wacc[3], dwacc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    wacc[k] = dwacc[k] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 4 * Q; ++c) acc[k][c] = dacc[k][c] = 0.0f;
+  }
+  for (int l = 0; l < L; ++l) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const int u = j / 3 - 1, v = j % 3 - 1;
+      const int sx = px - u, sy = py - v;
+      if (sx < 0 || sy < 0 || sx >= W || sy >= H) continue;
+      const int s = p - v * kRS - u;
+      if (!((fgm[s] >> l) & 1u)) continue;
+      const int sj = surface_index(zs, s, p, L);
+      const int k = sj > l ? 0 : (sj == l ? 1 : 2);
+      const float w = __fmul_rn(wx[(l * 3 + u + 1) * kRR + s], wy[(l * 3 + v + 1) * kRR + s]);
+      const float4 t = tg[l * kRR + s];
+      const float dw = 4.0f * w * ((t.x + float(u)) * t.z + (t.y + float(v)) * t.w);
+#pragma unroll
+      for (int g = 0; g < Q; ++g) {
+        const float4 c = col[(l * Q + g) * kRR + s], dc = dcol[(l * Q + g) * kRR + s];
+        const float cv[4] = {c.x, c.y, c.z, c.w}, dcv[4] = {dc.x, dc.y, dc.z, dc.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          acc[k][4 * g + h] = fmaf(w, cv[h], acc[k][4 * g + h]);
+          dacc[k][4 * g + h] = fmaf(dw, cv[h], fmaf(w, dcv[h], dacc[k][4 * g + h]));
+        }
+      }
+      wacc[k] += w;
+      dwacc[k] += dw;
+    }
+  }
+  float n[3][C], dn[3][C];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float sc = norm_scale(wacc[k]);
+    const float x = wacc[k] - 1.0f;
+    const float gate = x > 0.0f ? 1.0f : (x == 0.0f ? 0.5f : 0.0f);
+    const float dsc = -sc * sc * gate * dwacc[k];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      n[k][c] = acc[k][c] * sc;
+      dn[k][c] = dacc[k][c] * sc + acc[k][c] * dsc;
+    }
+  }
+  // out = n0 + (1 - a0) (n1 + (1 - a1) n2), a_k = n_k[C - 1]
+  const float a0 = n[0][C - 1], a1 = n[1][C - 1];
+  const float da0 = dn[0][C - 1], da1 = dn[1][C - 1];
+  float o[4 * Q];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const float mid = n[1][c] + (1.0f - a1) * n[2][c];
+    const float dmid = dn[1][c] - da1 * n[2][c] + (1.0f - a1) * dn[2][c];
+    o[c] = dn[0][c] - da0 * mid + (1.0f - a0) * dmid;
+  }
+  const int64_t pix = B.pix_off[tr.img] + int64_t(py) * W + px;
+  store_row<C>(d_image + pix * C, o);
+}
+
 float gaussian_coef() {
   // (1 + 0.05) / sum_{u,v in {-1,0,1}} exp(-2 (u^2 + v^2)), in double then
   // rounded to float as the reference's weakly typed constant (splat.py:63-78).
@@ -1141,6 +1276,36 @@ int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
     if (tiles > 0) kern<<<tiles, kTX * kTY, smem, stream>>>(a, b);
   }
   return launch_status(bwd ? "splat backward" : "splat", err);
+}
+
+
+size_t jvp_smem(int L, int C) {
+  return size_t(L) * kRR * 4 * (7 + 4 + 8 * ((C + 3) / 4)) + size_t(kRR) * 2;
+}
+
+template <int C>
+int run_splat_jvp(const SplatArgs& a, const float4* d_vp, const float* d_colors,
+                  float* d_image, const dr_image_desc* images, int n, cudaStream_t stream,
+                  std::string& err) {
+  const size_t smem = jvp_smem(a.L, C);
+  static size_t reserved = 0;
+  if (smem > 48 * 1024 && smem > reserved) {
+    if (cudaFuncSetAttribute(splat_jvp_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem)) != cudaSuccess) {
+      err = "layers x channels need more shared memory than the device has";
+      return DR_ERR_INVALID_ARGUMENT;
+    }
+    reserved = smem;
+  }
+  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+    Batch b;
+    if (!make_batch(images + g0, cnt, a.L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
+    const int tiles = b.tile_start[cnt];
+    if (tiles > 0)
+      splat_jvp_kernel<C><<<tiles, kTX * kTY, smem, stream>>>(a, d_vp, d_colors, d_image, b);
+  }
+  return launch_status("splat jvp", err);
 }
 
 int dispatch(bool bwd, int C, const SplatArgs& a, const dr_image_desc* images, int n,
@@ -1358,6 +1523,50 @@ int splat_bwd_launch(const float* d_out, const float* positions, const float* z_
   a.d_out = d_out; a.d_colors = d_colors;
   a.d_vp = reinterpret_cast<float4*>(d_positions);
   return dispatch(true, C, a, images, n, stream, err);
+}
+
+
+int splat_jvp_launch(const float* positions, const float* z_buffer, const float* colors,
+                     const float* d_positions, const float* d_colors, int C,
+                     const dr_image_desc* images, int n, int L, float* d_image,
+                     cudaStream_t stream, std::string& err) {
+  int rc;
+  if (!check_batch(L, n, images, err, rc)) return rc;
+  if (!positions || !colors || !d_image) {
+    err = "positions, colors and d_image must be non-null";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  if (jvp_smem(L, C) > 227 * 1024) {
+    err = "layers x channels need more shared memory than the device has";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  if (!aligned16({positions, d_positions}) ||
+      (C % 4 == 0 && !aligned16({colors, d_colors, d_image}))) {
+    err = "positions, d_positions (and, with a multiple of 4 channels, colors, d_colors "
+          "and d_image) must be 16-byte aligned";
+    return DR_ERR_MISALIGNED;
+  }
+  SplatArgs a{};
+  a.vp = reinterpret_cast<const float4*>(positions);
+  a.zb = z_buffer;
+  a.colors = colors;
+  a.L = L;
+  a.P = call_pixels(images, n);
+  a.coef = gaussian_coef();
+  const float4* dvp = reinterpret_cast<const float4*>(d_positions);
+  switch (C) {
+    case 1: return run_splat_jvp<1>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 2: return run_splat_jvp<2>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 3: return run_splat_jvp<3>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 4: return run_splat_jvp<4>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 5: return run_splat_jvp<5>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 6: return run_splat_jvp<6>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 7: return run_splat_jvp<7>(a, dvp, d_colors, d_image, images, n, stream, err);
+    case 8: return run_splat_jvp<8>(a, dvp, d_colors, d_image, images, n, stream, err);
+    default:
+      err = "splat supports 1 to 8 channels";
+      return DR_ERR_INVALID_ARGUMENT;
+  }
 }
 
 }  // namespace dr

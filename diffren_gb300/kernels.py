@@ -262,8 +262,26 @@ class _Transform(torch.autograd.Function):
                                        _p(clip), _stream(vertices.device))
       _lib.check(rc, "dr_transform_vertices")
     ctx.save_for_backward(vertices, matrices)
+    ctx.save_for_forward(vertices, matrices)
     ctx.batch = batch
     return clip
+
+  @staticmethod
+  def jvp(ctx, d_vertices, d_matrices, _):
+    vertices, matrices = ctx.saved_tensors
+    batch = ctx.batch
+    d_clip = torch.zeros(vertices.shape[0], 4, dtype=torch.float32, device=vertices.device)
+    if d_vertices is not None:
+      dv = d_vertices.float()
+      if dv.shape[1] == 3:  # the tangent of the homogeneous 1 is 0
+        dv = torch.cat([dv, torch.zeros_like(dv[:, :1])], 1)
+      d_clip = _Transform.apply(dv.contiguous(), matrices, batch)
+    if d_matrices is not None:
+      idx = batch.vertex_image_index(vertices.device)
+      vh = vertices if vertices.shape[1] == 4 else torch.cat(
+          [vertices, torch.ones_like(vertices[:, :1])], dim=1)
+      d_clip = d_clip + torch.einsum("vj,vij->vi", vh, d_matrices.float()[idx])
+    return d_clip
 
   @staticmethod
   def backward(ctx, d_clip):
@@ -469,10 +487,41 @@ class _RasterSamples(torch.autograd.Function):
           _stream(dev))
     _lib.check(rc, "dr_rasterize_batch_interpolate")
     ctx.save_for_backward(attributes, clip, bary, triangles, ids, z, vp, vids)
-    ctx.batch, ctx.L = batch, L
+    ctx.save_for_forward(bary, triangles, ids, z, vp)
+    ctx.batch, ctx.L, ctx.num_channels = batch, L, K
     ctx.set_materialize_grads(False)
     ctx.mark_non_differentiable(ids, z, bary)
     return out, vp, ids, z, bary
+
+  @staticmethod
+  def jvp(ctx, d_attributes, d_clip, *unused):
+    """Tangents of the interpolated attributes and the splat positions at
+    fixed barycentrics (the rasterizer's outputs carry no derivative)."""
+    bary, triangles, ids, z, vp = ctx.saved_tensors
+    batch, L = ctx.batch, ctx.L
+    n = ids.shape[0]
+    K = ctx.num_channels
+    if d_attributes is not None:
+      d_out = interpolate_packed(d_attributes.detach(), bary, triangles, ids, z, batch, L)
+    else:
+      d_out = torch.zeros(n, K, dtype=torch.float32, device=ids.device)
+    d_vp = torch.zeros(n, 4, dtype=torch.float32, device=ids.device)
+    if d_clip is not None:
+      # vp = ((c.xyz / c.w) + 1) (W, H, 1) / 2 with c the interpolated clip
+      # position (vp.w = c.w): d vp = (d c.xyz - ndc d c.w) / c.w (W, H, 1) / 2.
+      dc = interpolate_packed(d_clip.detach(), bary, triangles, ids, z, batch, L)
+      for i in range(batch.n):
+        half = torch.tensor([batch.widths[i] * 0.5, batch.heights[i] * 0.5, 0.5],
+                            dtype=torch.float32, device=ids.device)
+        q = batch.layered_view(vp, i, L).reshape(-1, 4)
+        d = batch.layered_view(dc, i, L).reshape(-1, 4)
+        fg = (batch.layered_view(z, i, L).reshape(-1) != 1.0)[:, None]
+        ndc = q[:, :3] / half - 1.0
+        w = torch.where(fg, q[:, 3:4], torch.ones_like(q[:, 3:4]))
+        t = (d[:, :3] - ndc * d[:, 3:4]) / w * half
+        t = torch.where(fg, torch.cat([t, d[:, 3:4]], 1), torch.zeros_like(d))
+        batch.layered_view(d_vp, i, L).copy_(t.view_as(batch.layered_view(d_vp, i, L)))
+    return d_out, d_vp, None, None, None
 
   @staticmethod
   def backward(ctx, d_out, d_vp, *unused):
@@ -571,11 +620,30 @@ class _Splat(torch.autograd.Function):
                             _p(out), _p(saved), _p(accum), _p(norm), _stream(dev))
     _lib.check(rc, "dr_splat_fwd")
     ctx.save_for_backward(positions, colors, saved, z)
+    ctx.save_for_forward(positions, colors, z)
     ctx.batch, ctx.L = batch, L
+    ctx.want_accum = want_accum
     if want_accum:
       ctx.mark_non_differentiable(accum, norm)
       return out, accum, norm
     return out
+
+  @staticmethod
+  def jvp(ctx, d_positions, d_colors, *unused):
+    """Tangent of the image (discrete state held fixed), by dr_splat_jvp."""
+    positions, colors, z = ctx.saved_tensors
+    lib = _lib.load()
+    C = colors.shape[1]
+    d_image = torch.empty(ctx.batch.total_pixels, C, dtype=torch.float32, device=colors.device)
+    dp = d_positions.float().contiguous() if d_positions is not None else None
+    dc = d_colors.float().contiguous() if d_colors is not None else None
+    with _op("splat_jvp", _groups(ctx.batch)):
+      rc = lib.dr_splat_jvp(_p(positions), _p(z), _p(colors), _p(dp), _p(dc), C, ctx.batch.ptr,
+                            ctx.batch.n, ctx.L, _p(d_image), _stream(colors.device))
+    _lib.check(rc, "dr_splat_jvp")
+    if ctx.want_accum:
+      return d_image, None, None
+    return d_image
 
   @staticmethod
   def backward(ctx, d_out, *unused):

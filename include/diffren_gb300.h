@@ -45,9 +45,9 @@
  *       composite.py:20-37) and its VJP.
  *   dr_vertex_normals_fwd/bwd -> utils.mesh.compute_vertex_normals
  *       (diffren/jax/utils/mesh.py:22-52) and its VJP.
- *   dr_splat_fwd/bwd        -> splat.splat_at_pixel_centers + composite.over
+ *   dr_splat_fwd/bwd/jvp    -> splat.splat_at_pixel_centers + composite.over
  *       (diffren/jax/internal/splat.py:26-175, diffren/jax/composite.py:20-37)
- *       and their VJP.
+ *       and their VJP and JVP.
  */
 #ifndef DIFFREN_GB300_H_
 #define DIFFREN_GB300_H_
@@ -396,6 +396,17 @@ int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buff
                  const float* colors, const float* saved, int32_t num_channels,
                  const dr_image_desc* images, int32_t num_images, int32_t num_layers,
                  float* d_colors, float* d_positions, void* stream);
+
+/* Forward-mode derivative of dr_splat_fwd's image for tangents of the
+ * positions (d_positions [L, H, W, 4], x and y read) and, when non-null, of
+ * the colors (d_colors [L, H, W, C]), with the discrete state (pixel floors,
+ * surface classes, foreground) held fixed: the jax.jvp of
+ * splat_at_pixel_centers + composite.over (splat.py:26-175,
+ * composite.py:20-37). Writes d_image [H, W, C]. */
+int dr_splat_jvp(const float* positions, const float* z_buffer, const float* colors,
+                 const float* d_positions, const float* d_colors, int32_t num_channels,
+                 const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                 float* d_image, void* stream);
 
 #ifdef __cplusplus
 }

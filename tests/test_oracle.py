@@ -359,3 +359,39 @@ def test_oracle_spot_lighting_goldens(lighting):
   out = (lit * (z != 1.0)[..., None])[0]  # OVER of one masked layer
   ok, msg = helpers.images_near_python(g[lighting], helpers.pil_format(out))
   assert ok, msg
+
+
+def test_oracle_spike_derivative_golden():
+  """splat_test.py:170-224: the forward-mode derivative (jax.jvp) of a
+  render with respect to the offset of one sphere vertex, through the torch
+  restatement (torch.func.jvp in place of jax.jvp, discrete state held
+  fixed), equals the reference's Spike_Derivative.png. Pins the derivative
+  of the splat chain to the reference's own output."""
+  g = helpers.golden("render_goldens.npz")
+  v0 = g["sphere_vertices"].astype(np.float32)
+  t = g["sphere_triangles"].astype(np.int32)
+  v = v0.copy()
+  v[32] *= 2.0
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("view_1")
+  W, H = helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT
+  clip32 = raster.transform(proj.astype(np.float32), v)
+  ids, z, b = raster.rasterize(clip32, t, W, H, 1, 1)
+  state = torch_ref.discrete_state(clip32, ids, z, b, t, W, H)
+  ti, tz, tt, tb = torch.tensor(ids), torch.tensor(z), torch.tensor(t).long(), torch.tensor(b)
+  P = torch.tensor(proj, dtype=torch.float32)
+  ones = torch.ones(len(v), 4)
+
+  def render(vv):
+    clip = torch.cat([vv, torch.ones_like(vv[:, :1])], 1) @ P.T
+    shaded = torch_ref.interpolate(ones, ti, tz, tb, tt)
+    return torch_ref.splat_shaded_pixels(clip, ti, tz, tb, tt, shaded, W, H, state)[0]
+
+  tangent = torch.zeros(len(v), 3)
+  tangent[32] = torch.tensor(v0[32])  # d vertices / d offset
+  rendered, jac = torch.func.jvp(render, (torch.tensor(v),), (tangent,))
+  image = (jac / jac.abs().max()) * 0.5 + 0.5
+  image = image * 0.95 + rendered * 0.05
+  ok, msg = helpers.images_near_python(g["spike_derivative"],
+                                       helpers.pil_format(image[..., :3].numpy()),
+                                       threshold=0.0)
+  assert ok, msg

@@ -300,3 +300,65 @@ def test_point_light_on_vertex_normals_matches_oracle(device):
     want = want.numpy()
     scale = float(np.abs(want).max())
     np.testing.assert_allclose(ours.cpu().numpy(), want, rtol=1e-4, atol=1e-4 * scale)
+
+
+def _spike_scene(device):
+  v0 = G["sphere_vertices"].astype(np.float32)
+  t = torch.tensor(G["sphere_triangles"].astype(np.int32), device=device)
+  proj = helpers.make_perspective_matrix() @ helpers.make_look_at_matrix("view_1")
+  return v0, t, torch.tensor(proj, dtype=torch.float32, device=device)
+
+
+def test_spike_derivative_golden(device):
+  """splat_test.py:170-224: forward-mode derivative (torch.autograd.forward_ad
+  in place of jax.jvp) of render_triangles with respect to the offset of one
+  sphere vertex, through the CUDA JVP kernels, against Spike_Derivative.png
+  (no pixel may differ beyond the reference's 0.5% outlier allowance)."""
+  import torch.autograd.forward_ad as fwAD
+  v0, t, proj = _spike_scene(device)
+  v = v0.copy()
+  v[32] *= 2.0
+  tangent = torch.zeros(len(v), 3, device=device)
+  tangent[32] = torch.tensor(v0[32], device=device)
+  colors = torch.ones(len(v), 4, device=device)
+  with fwAD.dual_level():
+    vd = fwAD.make_dual(torch.tensor(v, device=device), tangent)
+    out = render.render_triangles(vd, {"colors": colors}, t, proj, helpers.IMAGE_WIDTH,
+                                  helpers.IMAGE_HEIGHT, lambda a: a["colors"])
+    rendered, jac = fwAD.unpack_dual(out)
+  image = (jac / jac.abs().max()) * 0.5 + 0.5
+  image = image * 0.95 + rendered * 0.05
+  ok, msg = helpers.images_near_python(G["spike_derivative"],
+                                       helpers.pil_format(image[..., :3].cpu().numpy()),
+                                       threshold=0.0)
+  assert ok, msg
+
+
+def test_jvp_agrees_with_vjp(device):
+  """<J t, g> = <t, J^T g> through render_triangles (3 layers, color and
+  vertex tangents): the forward-mode kernels and the VJP kernels compute the
+  same derivative."""
+  import torch.autograd.forward_ad as fwAD
+  m = workloads.icosphere_workload(8, seed=6)
+  cam = torch.tensor(workloads.camera_matrix((0.5, 0.4, 2.7), 96, 80), device=device)
+  v = torch.tensor(m.vertices, device=device)
+  c = torch.tensor(m.colors, device=device)
+  t = torch.tensor(m.triangles, device=device)
+  rng = np.random.default_rng(3)
+  tv = torch.tensor(rng.standard_normal(v.shape), dtype=torch.float32, device=device) * 0.01
+  tc = torch.tensor(rng.standard_normal(c.shape), dtype=torch.float32, device=device)
+
+  def shade(a):
+    return torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1)
+
+  with fwAD.dual_level():
+    out = render.render_triangles(fwAD.make_dual(v, tv), {"rgb": fwAD.make_dual(c, tc)}, t,
+                                  cam, 96, 80, shade, num_layers=3)
+    _, jt = fwAD.unpack_dual(out)
+  g = torch.tensor(rng.standard_normal(tuple(jt.shape)), dtype=torch.float32, device=device)
+  vr, cr = v.clone().requires_grad_(True), c.clone().requires_grad_(True)
+  out2 = render.render_triangles(vr, {"rgb": cr}, t, cam, 96, 80, shade, num_layers=3)
+  gv, gc = torch.autograd.grad(out2, (vr, cr), g)
+  lhs = float((jt.double() * g.double()).sum())
+  rhs = float((tv.double() * gv.double()).sum() + (tc.double() * gc.double()).sum())
+  assert abs(lhs - rhs) <= 1e-4 * max(abs(lhs), abs(rhs)), (lhs, rhs)
