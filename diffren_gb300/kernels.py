@@ -331,7 +331,26 @@ class _Interpolate(torch.autograd.Function):
                                 _p(out), _stream(ids.device))
     _lib.check(rc, "dr_interpolate_fwd")
     ctx.save_for_backward(attributes, bary, triangles, ids, z)
+    ctx.save_for_forward(attributes, bary, triangles, ids, z)
     ctx.batch, ctx.L, ctx.has_bg = batch, L, background is not None
+    return out
+
+  @staticmethod
+  def jvp(ctx, d_attr, d_bary, d_bg, *unused):
+    """fg (sum_i b_i a_i) + (1 - fg) bg is linear in the attributes, the
+    barycentrics and the background separately."""
+    attributes, bary, triangles, ids, z = ctx.saved_tensors
+    batch, L = ctx.batch, ctx.L
+    out = torch.zeros(ids.shape[0], attributes.shape[1], dtype=torch.float32,
+                      device=ids.device)
+    if d_attr is not None:
+      out = out + _Interpolate.apply(d_attr.detach().float().contiguous(), bary, None,
+                                     triangles, ids, z, batch, L)
+    if d_bary is not None:
+      out = out + _Interpolate.apply(attributes, d_bary.detach().float().contiguous(), None,
+                                     triangles, ids, z, batch, L)
+    if d_bg is not None:
+      out = out + (z == 1.0).float()[:, None] * d_bg.detach().float()
     return out
 
   @staticmethod
@@ -461,6 +480,31 @@ def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, wa
   return d_attr, d_clip, d_bary
 
 
+def _viewport_tangent(q, dc, z, batch, L, w_from_vp):
+  """Tangent of the splat positions vp = ((c.xyz / c.w) + 1) (W, H, 1) / 2
+  (splat.py:207-221) for a tangent dc of the interpolated clip position c:
+  d vp.xyz = (dc.xyz - ndc dc.w) / c.w (W, H, 1) / 2; background samples get
+  0. With w_from_vp, q is the fused rasterizer's positions (viewport xyz,
+  clip w); otherwise q is the interpolated clip position c itself. The
+  tangent's w is dc.w (the clip w) with w_from_vp, else 0 (the foreground
+  flag)."""
+  d_vp = torch.zeros(q.shape[0], 4, dtype=torch.float32, device=q.device)
+  for i in range(batch.n):
+    half = torch.tensor([batch.widths[i] * 0.5, batch.heights[i] * 0.5, 0.5],
+                        dtype=torch.float32, device=q.device)
+    qi = batch.layered_view(q, i, L).reshape(-1, 4)
+    d = batch.layered_view(dc, i, L).reshape(-1, 4)
+    fg = (batch.layered_view(z, i, L).reshape(-1) != 1.0)[:, None]
+    w = torch.where(fg, qi[:, 3:4], torch.ones_like(qi[:, 3:4]))
+    ndc = qi[:, :3] / half - 1.0 if w_from_vp else qi[:, :3] / w
+    t = (d[:, :3] - ndc * d[:, 3:4]) / w * half
+    t = torch.cat([t, d[:, 3:4] if w_from_vp else torch.zeros_like(t[:, :1])], 1)
+    t = torch.where(fg, t, torch.zeros_like(t))
+    dst = batch.layered_view(d_vp, i, L)
+    dst.copy_(t.view_as(dst))
+  return d_vp
+
+
 class _RasterSamples(torch.autograd.Function):
   """Rasterization fused with attribute interpolation and splat positions;
   the VJP is that of the fused pass (the rasterizer's own outputs carry no
@@ -505,22 +549,12 @@ class _RasterSamples(torch.autograd.Function):
       d_out = interpolate_packed(d_attributes.detach(), bary, triangles, ids, z, batch, L)
     else:
       d_out = torch.zeros(n, K, dtype=torch.float32, device=ids.device)
-    d_vp = torch.zeros(n, 4, dtype=torch.float32, device=ids.device)
     if d_clip is not None:
-      # vp = ((c.xyz / c.w) + 1) (W, H, 1) / 2 with c the interpolated clip
-      # position (vp.w = c.w): d vp = (d c.xyz - ndc d c.w) / c.w (W, H, 1) / 2.
       dc = interpolate_packed(d_clip.detach(), bary, triangles, ids, z, batch, L)
-      for i in range(batch.n):
-        half = torch.tensor([batch.widths[i] * 0.5, batch.heights[i] * 0.5, 0.5],
-                            dtype=torch.float32, device=ids.device)
-        q = batch.layered_view(vp, i, L).reshape(-1, 4)
-        d = batch.layered_view(dc, i, L).reshape(-1, 4)
-        fg = (batch.layered_view(z, i, L).reshape(-1) != 1.0)[:, None]
-        ndc = q[:, :3] / half - 1.0
-        w = torch.where(fg, q[:, 3:4], torch.ones_like(q[:, 3:4]))
-        t = (d[:, :3] - ndc * d[:, 3:4]) / w * half
-        t = torch.where(fg, torch.cat([t, d[:, 3:4]], 1), torch.zeros_like(d))
-        batch.layered_view(d_vp, i, L).copy_(t.view_as(batch.layered_view(d_vp, i, L)))
+      # vp.w holds the clip w here, and xyz/w = 2 vp.xyz / (W, H, 1) - 1.
+      d_vp = _viewport_tangent(vp, dc, z, batch, L, w_from_vp=True)
+    else:
+      d_vp = torch.zeros(n, 4, dtype=torch.float32, device=ids.device)
     return d_out, d_vp, None, None, None
 
   @staticmethod
@@ -571,8 +605,22 @@ class _Positions(torch.autograd.Function):
                                       batch.ptr, batch.n, L, _p(vp), _stream(ids.device))
     _lib.check(rc, "dr_splat_positions_fwd")
     ctx.save_for_backward(clip, bary, triangles, ids, z)
+    ctx.save_for_forward(clip, bary, triangles, ids, z)
     ctx.batch, ctx.L = batch, L
     return vp
+
+  @staticmethod
+  def jvp(ctx, d_clip, d_bary, *unused):
+    clip, bary, triangles, ids, z = ctx.saved_tensors
+    batch, L = ctx.batch, ctx.L
+    c = interpolate_packed(clip, bary, triangles, ids, z, batch, L)
+    dc = torch.zeros_like(c)
+    if d_clip is not None:
+      dc = dc + interpolate_packed(d_clip.detach(), bary, triangles, ids, z, batch, L)
+    if d_bary is not None:
+      dc = dc + interpolate_packed(clip, d_bary.detach().contiguous(), triangles, ids, z,
+                                   batch, L)
+    return _viewport_tangent(c, dc, z, batch, L, w_from_vp=False)
 
   @staticmethod
   def backward(ctx, d_vp):

@@ -334,10 +334,12 @@ def test_spike_derivative_golden(device):
   assert ok, msg
 
 
-def test_jvp_agrees_with_vjp(device):
+@pytest.mark.parametrize("wide", [False, True])
+def test_jvp_agrees_with_vjp(wide, device):
   """<J t, g> = <t, J^T g> through render_triangles (3 layers, color and
   vertex tangents): the forward-mode kernels and the VJP kernels compute the
-  same derivative."""
+  same derivative, on the fused path and (more than 16 attribute channels)
+  on the separate interpolation and positions kernels."""
   import torch.autograd.forward_ad as fwAD
   m = workloads.icosphere_workload(8, seed=6)
   cam = torch.tensor(workloads.camera_matrix((0.5, 0.4, 2.7), 96, 80), device=device)
@@ -348,16 +350,19 @@ def test_jvp_agrees_with_vjp(device):
   tv = torch.tensor(rng.standard_normal(v.shape), dtype=torch.float32, device=device) * 0.01
   tc = torch.tensor(rng.standard_normal(c.shape), dtype=torch.float32, device=device)
 
+  extra = {"pad": torch.zeros(len(m.vertices), 14, device=device)} if wide else {}
+
   def shade(a):
     return torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1)
 
   with fwAD.dual_level():
-    out = render.render_triangles(fwAD.make_dual(v, tv), {"rgb": fwAD.make_dual(c, tc)}, t,
-                                  cam, 96, 80, shade, num_layers=3)
+    out = render.render_triangles(fwAD.make_dual(v, tv),
+                                  {"rgb": fwAD.make_dual(c, tc), **extra}, t, cam, 96, 80,
+                                  shade, num_layers=3)
     _, jt = fwAD.unpack_dual(out)
   g = torch.tensor(rng.standard_normal(tuple(jt.shape)), dtype=torch.float32, device=device)
   vr, cr = v.clone().requires_grad_(True), c.clone().requires_grad_(True)
-  out2 = render.render_triangles(vr, {"rgb": cr}, t, cam, 96, 80, shade, num_layers=3)
+  out2 = render.render_triangles(vr, {"rgb": cr, **extra}, t, cam, 96, 80, shade, num_layers=3)
   gv, gc = torch.autograd.grad(out2, (vr, cr), g)
   lhs = float((jt.double() * g.double()).sum())
   rhs = float((tv.double() * gv.double()).sum() + (tc.double() * gc.double()).sum())
