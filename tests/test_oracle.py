@@ -361,6 +361,7 @@ def test_oracle_spot_lighting_goldens(lighting):
   assert ok, msg
 
 
+@pytest.mark.filterwarnings("ignore::DeprecationWarning")  # torch.func's own imports
 def test_oracle_spike_derivative_golden():
   """splat_test.py:170-224: the forward-mode derivative (jax.jvp) of a
   render with respect to the offset of one sphere vertex, through the torch
