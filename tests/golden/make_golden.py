@@ -203,6 +203,10 @@ def main():
   imgs.update(textured_square_inputs(os.path.join(ref, "diffren", "jax", "utils",
                                                    "shaders_test.py")))
   imgs["sphere_disparity"] = png.read_png(os.path.join(data, "Sphere_Disparity.png"))
+  # rasterize_test.py:28-152 (barycentrics of one triangle, w constant or varying)
+  imgs["simple_triangle"] = png.read_png(os.path.join(data, "Simple_Triangle.png"))
+  imgs["perspective_corrected_triangle"] = png.read_png(
+      os.path.join(data, "Perspective_Corrected_Triangle.png"))
   np.savez_compressed(os.path.join(HERE, "render_goldens.npz"), **imgs)
 
   # The textured spot of splat_test.py:227-277: the mesh flattened and scaled

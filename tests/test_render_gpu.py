@@ -367,3 +367,26 @@ def test_jvp_agrees_with_vjp(wide, device):
   lhs = float((jt.double() * g.double()).sum())
   rhs = float((tv.double() * gv.double()).sum() + (tc.double() * gc.double()).sum())
   assert abs(lhs - rhs) <= 1e-4 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("w_vector,golden,none_camera,diff_barys", [
+    ([1.0, 1.0, 1.0], "simple_triangle", False, False),
+    ([1.0, 1.0, 1.0], "simple_triangle", False, True),
+    ([1.0, 1.0, 1.0], "simple_triangle", True, False),
+    ([0.2, 0.5, 2.0], "perspective_corrected_triangle", False, False),
+    ([0.2, 0.5, 2.0], "perspective_corrected_triangle", False, True),
+])
+def test_rasterize_simple_triangle_goldens(w_vector, golden, none_camera, diff_barys, device):
+  """rasterize_test.py:28-152: barycentrics of one triangle through
+  rasterize.rasterize_triangles (identity or no camera, w constant or
+  varying, with and without differentiable barycentrics)."""
+  clip = torch.tensor([[-0.5, -0.5, 0.8, 1.0], [0.0, 0.5, 0.3, 1.0], [0.5, -0.5, 0.3, 1.0]],
+                      device=device) * torch.tensor(w_vector, device=device)[:, None]
+  camera = None if none_camera else torch.eye(4, device=device)
+  fb = rasterize.rasterize_triangles(clip, torch.tensor([[0, 1, 2]], device=device), camera,
+                                     helpers.IMAGE_WIDTH, helpers.IMAGE_HEIGHT,
+                                     compute_diff_barys=diff_barys)
+  b = fb.barycentrics[0].detach().cpu().numpy()
+  image = np.concatenate([b, np.ones_like(b[..., :1])], -1)
+  ok, msg = helpers.images_near_python(helpers.to_rgba(G[golden]), helpers.pil_format(image))
+  assert ok, msg
