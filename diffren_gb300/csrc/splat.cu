@@ -224,7 +224,6 @@ __device__ __forceinline__ float4 run_sum4(float4 v, int lane, int last) {
                      run_sum(v.z, lane, last), run_sum(v.w, lane, last));
 }
 
-constexpr int kMaxRuns = 4;  // sum runs when a warp has at most this many
 constexpr int kVjpThreads = 512;
 constexpr int kVjpPerThread = 8;  // samples whose depth each thread tests
 constexpr int kVjpBlock = kVjpThreads * kVjpPerThread;
@@ -353,10 +352,10 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
         }
       }
     }
-    // Runs of lanes with the same image and the same three vertex rows.
-    // Warps with many short runs (small triangles) skip the summation:
-    // their atomics rarely collide.
-    // (All four shuffles run on every lane before any comparison.)
+    // Runs of lanes with the same image and the same three vertex rows are
+    // summed by shuffles and only each run's first lane issues the atomics
+    // (measured faster than atomics from every lane even for warps of many
+    // short runs). All four shuffles run on every lane before any comparison.
     const int kim = on ? im : -1;
     const int p_im = __shfl_up_sync(0xffffffffu, kim, 1);
     const int p_v0 = __shfl_up_sync(0xffffffffu, vid[0], 1);
@@ -365,20 +364,17 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
     const bool differs = (kim != p_im) | (vid[0] != p_v0) | (vid[1] != p_v1) | (vid[2] != p_v2);
     (void)id;
     const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || differs);
-    const bool combine = __popc(heads) <= kMaxRuns;
     const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
-    const int last = combine ? (later ? __ffs(later) - 2 : 31) : lane;
-    const bool leader = combine ? ((heads >> lane) & 1u) != 0 : true;
+    const int last = later ? __ffs(later) - 2 : 31;
+    const bool leader = ((heads >> lane) & 1u) != 0;
     float db[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const float bi = b[i];
       float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
-      if (combine) {
-        cv.x = run_sum(cv.x, lane, last);
-        cv.y = run_sum(cv.y, lane, last);
-        cv.w = run_sum(cv.w, lane, last);
-      }
+      cv.x = run_sum(cv.x, lane, last);
+      cv.y = run_sum(cv.y, lane, last);
+      cv.w = run_sum(cv.w, lane, last);
       if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
         atomicAdd(p.d_clip + B.vertex_offset[im] + vid[i], cv);
       db[i] = on ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
@@ -395,7 +391,7 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
         for (int i = 0; i < 3; ++i) {
           const float bi = b[i];
           float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
-          if (combine) av = run_sum4(av, lane, last);
+          av = run_sum4(av, lane, last);
           const int64_t row = aoff + int64_t(vid[i]) * K + kk;
           if (leader && on) add_chunk(a.d_attr + row, av, nc, vec_rows);
           if (on && p.d_bary) {
