@@ -401,8 +401,69 @@ class _DiffBary(torch.autograd.Function):
                                       _stream(ids.device))
     _lib.check(rc, "dr_diff_barycentrics_fwd")
     ctx.save_for_backward(clip, triangles, ids, z)
+    ctx.save_for_forward(clip, triangles, ids, z)
     ctx.batch, ctx.L = batch, L
     return bary
+
+  @staticmethod
+  def jvp(ctx, d_clip, *unused):
+    """Tangent of the barycentrics (rasterize.py:127-255) for clip-vertex
+    tangents, image by image in torch ops: the adjugate's cofactors by the
+    product rule, u = M p, b = u / sum(u) by the quotient rule (0 where the
+    barycentrics are not finite). Forward mode only; the VJP kernel serves
+    reverse mode."""
+    clip, triangles, ids, z = ctx.saved_tensors
+    batch, L = ctx.batch, ctx.L
+    out = torch.zeros(ids.shape[0], 3, dtype=torch.float32, device=ids.device)
+    if d_clip is None:
+      return out
+    for i in range(batch.n):
+      W, H = batch.widths[i], batch.heights[i]
+      desc = batch.descs[i]
+      v0, nv = int(desc.vertex_offset), int(desc.num_vertices)
+      t0, nt = int(desc.triangle_offset), int(desc.num_triangles)
+      if nt == 0 or nv == 0:
+        continue
+      ids_i = batch.layered_view(ids, i, L).reshape(-1).long().clamp(0, nt - 1)
+      fg = (batch.layered_view(z, i, L).reshape(-1) != 1.0)[:, None].float()
+      pix = torch.arange(L * H * W, device=ids.device) % (H * W)
+      px = ((2 * (pix % W) + 1).float() / W - 1.0)[:, None]
+      py = ((2 * (pix // W) + 1).float() / H - 1.0)[:, None]
+      tri = triangles[t0:t0 + nt].long()
+
+      v = clip[v0:v0 + nv][tri]  # [T, 3, 4]
+      dv = d_clip[v0:v0 + nv].float()[tri]
+
+      def cof(a, b, c, e, da, db_, dc, de):
+        """a b - c e and its tangent."""
+        return a * b - c * e, da * b + a * db_ - dc * e - c * de
+
+      x, y, w = v[..., 0].unbind(-1), v[..., 1].unbind(-1), v[..., 3].unbind(-1)
+      dx, dy, dw = dv[..., 0].unbind(-1), dv[..., 1].unbind(-1), dv[..., 3].unbind(-1)
+      rows, drows = [], []
+      for i0, i1, i2 in ((0, 1, 2), (1, 2, 0), (2, 0, 1)):
+        # row i0 of the adjugate of [x; y; w] (cofactors of the other two)
+        e0 = cof(y[i1], w[i2], y[i2], w[i1], dy[i1], dw[i2], dy[i2], dw[i1])
+        e1 = cof(w[i1], x[i2], w[i2], x[i1], dw[i1], dx[i2], dw[i2], dx[i1])
+        e2 = cof(x[i1], y[i2], x[i2], y[i1], dx[i1], dy[i2], dx[i2], dy[i1])
+        rows.append(torch.stack([e0[0], e1[0], e2[0]], -1))
+        drows.append(torch.stack([e0[1], e1[1], e2[1]], -1))
+      d = torch.stack(rows, -2)
+      dd = torch.stack(drows, -2)
+      det = x[0] * d[:, 0, 0] + y[0] * d[:, 0, 1] + w[0] * d[:, 0, 2]
+      sign = torch.sign(det) + (det == 0).float()  # locally constant
+      m = (sign[:, None, None] * d)[ids_i]
+      dm = (sign[:, None, None] * dd)[ids_i]
+      u = m[..., 0] * px + m[..., 1] * py + m[..., 2]
+      du = dm[..., 0] * px + dm[..., 1] * py + dm[..., 2]
+      total = u.sum(-1, keepdim=True)
+      bary = u / total
+      db = (du - bary * du.sum(-1, keepdim=True)) / total
+      db = torch.where(torch.isfinite(bary) & torch.isfinite(db), db, torch.zeros_like(db))
+      db = db * fg
+      dst = batch.layered_view(out, i, L)
+      dst.copy_(db.view_as(dst))
+    return out
 
   @staticmethod
   def backward(ctx, d_bary):

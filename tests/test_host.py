@@ -107,3 +107,30 @@ def test_launch_counter():
   with kernels._op("x", 3):
     pass
   assert kernels.LAUNCHES.count == 3
+
+
+def test_diff_barycentrics_tangent_matches_oracle_forward_mode():
+  """The forward-mode rule of the differentiable barycentrics (torch ops,
+  runs on the CPU) against torch.func.jvp of the float64 restatement of
+  rasterize.py:127-255."""
+  import types
+  from oracle import raster, torch_ref
+  m = workloads.icosphere_workload(4, seed=1)
+  W, H, L = 24, 20, 2
+  clip = raster.transform(workloads.camera_matrix((0.3, 0.2, 2.5), W, H), m.vertices)
+  ids, z, _ = raster.rasterize(clip, m.triangles, W, H, L, 0)
+  batch = kernels.ImageBatch.single(W, H, len(m.vertices), len(m.triangles))
+  tc = torch.tensor(clip)
+  d_clip = torch.randn(tc.shape, generator=torch.Generator().manual_seed(0)) * 0.01
+  ctx = types.SimpleNamespace(
+      saved_tensors=(tc, torch.tensor(m.triangles), torch.tensor(ids).reshape(-1),
+                     torch.tensor(z).reshape(-1)), batch=batch, L=L)
+  got = kernels._DiffBary.jvp(ctx, d_clip)
+
+  def bary(c):
+    return torch_ref.diff_barycentrics(c, torch.tensor(ids), torch.tensor(z),
+                                       torch.tensor(m.triangles).long(), W, H)
+
+  _, want = torch.func.jvp(bary, (tc.double(),), (d_clip.double(),))
+  want = want.reshape(-1, 3)
+  assert float((got.double() - want).abs().max()) <= 1e-4 * float(want.abs().max())

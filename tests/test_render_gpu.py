@@ -334,12 +334,13 @@ def test_spike_derivative_golden(device):
   assert ok, msg
 
 
-@pytest.mark.parametrize("wide", [False, True])
-def test_jvp_agrees_with_vjp(wide, device):
+@pytest.mark.parametrize("wide,diff_barys", [(False, False), (True, False), (False, True)])
+def test_jvp_agrees_with_vjp(wide, diff_barys, device):
   """<J t, g> = <t, J^T g> through render_triangles (3 layers, color and
   vertex tangents): the forward-mode kernels and the VJP kernels compute the
-  same derivative, on the fused path and (more than 16 attribute channels)
-  on the separate interpolation and positions kernels."""
+  same derivative, on the fused path, on the separate interpolation and
+  positions kernels (more than 16 attribute channels) and with
+  differentiable barycentrics."""
   import torch.autograd.forward_ad as fwAD
   m = workloads.icosphere_workload(8, seed=6)
   cam = torch.tensor(workloads.camera_matrix((0.5, 0.4, 2.7), 96, 80), device=device)
@@ -358,11 +359,12 @@ def test_jvp_agrees_with_vjp(wide, device):
   with fwAD.dual_level():
     out = render.render_triangles(fwAD.make_dual(v, tv),
                                   {"rgb": fwAD.make_dual(c, tc), **extra}, t, cam, 96, 80,
-                                  shade, num_layers=3)
+                                  shade, num_layers=3, compute_diff_barys=diff_barys)
     _, jt = fwAD.unpack_dual(out)
   g = torch.tensor(rng.standard_normal(tuple(jt.shape)), dtype=torch.float32, device=device)
   vr, cr = v.clone().requires_grad_(True), c.clone().requires_grad_(True)
-  out2 = render.render_triangles(vr, {"rgb": cr, **extra}, t, cam, 96, 80, shade, num_layers=3)
+  out2 = render.render_triangles(vr, {"rgb": cr, **extra}, t, cam, 96, 80, shade, num_layers=3,
+                                 compute_diff_barys=diff_barys)
   gv, gc = torch.autograd.grad(out2, (vr, cr), g)
   lhs = float((jt.double() * g.double()).sum())
   rhs = float((tv.double() * gv.double()).sum() + (tc.double() * gc.double()).sum())
