@@ -146,18 +146,16 @@ def rgba(colors):
 
 
 def l2_loss_grads(out, target, params):
-  """L2 loss sum((out - target)^2) and HALF its gradients w.r.t. params.
+  """L2 loss sum((out - target)^2) and its gradients w.r.t. params.
 
-  d loss / d out = 2 (out - target). The VJP through the renderer is linear
-  in its seed, so seeding it with (out - target) yields exactly half of the
-  gradients (doubling is exact in float), without a pass over the images to
-  form 2 (out - target); the caller doubles the small per-vertex results.
+  One fused CUDA pass over the images gives the loss and d loss / d out =
+  2 (out - target) (`losses.squared_error_seed`), which seeds the renderer's
+  VJP directly: the gradients are the same bits as autograd of the loss.
   """
   import torch
-  diff = out.detach() - target
-  flat = diff.reshape(-1)
-  loss = torch.linalg.vecdot(flat, flat)
-  return loss, torch.autograd.grad(out, params, grad_outputs=diff)
+  from diffren_gb300 import losses
+  loss, seed = losses.squared_error_seed(out, target)
+  return loss, torch.autograd.grad(out, params, grad_outputs=seed)
 
 
 _L2 = []
@@ -297,6 +295,8 @@ def kernel_bytes(wl, fg, near=None, C=4, K=4):
       "texture_fwd": S * (8 + 4 * C),
       # its VJP: d color and uv in, d uv out (texture gradient atomics in L2)
       "texture_bwd": S * (4 * C + 8 + 8),
+      # L2 loss: image and target in, the VJP's seed out
+      "squared_error": 12 * C * P,
   }
 
 
@@ -342,9 +342,6 @@ def run_ours(args, rank, world, device):
   # one step on each set in turn while the other set's copies are in flight.
   sets = [dict(verts=verts_h.to(device), cols=cols_h.to(device), cams=cams_h.to(device))
           for _ in range(2)]
-  for b in sets:
-    b.update(g_v=torch.empty_like(b["verts"]), g_c=torch.empty_like(b["cols"]),
-             loss=torch.empty((), device=device))
   verts, cams = sets[0]["verts"], sets[0]["cams"]
 
   def step(b=sets[0]):
@@ -359,9 +356,7 @@ def run_ours(args, rank, world, device):
     else:
       out = r.render(v, {"rgba": rgba(c)}, cams, shader)
     loss, (gv, gc) = l2_loss_grads(out, target, (v, c))
-    torch.mul(gv, 2.0, out=b["g_v"])
-    torch.mul(gc, 2.0, out=b["g_c"])
-    b["loss"].copy_(loss)
+    return dict(g_v=gv, g_c=gc.contiguous(), loss=loss)
 
   # Eager warm-up on a side stream, then capture the step.
   s = torch.cuda.Stream(device)
@@ -385,16 +380,17 @@ def run_ours(args, rank, world, device):
       m = (r.batch.layered_view(z_fg, i, wl.num_layers) != 1.0).any(0).float()
       near += int(torch.nn.functional.max_pool2d(m[None, None], 3, 1, 1).sum())
   del z_fg
-  graph = torch.cuda.CUDAGraph()
-  with torch.cuda.graph(graph):
-    step(sets[0])
-  # The same step on the second buffer set, sharing the first graph's
-  # memory pool (the two graphs only ever replay one after the other on
-  # one stream).
-  graph_b = torch.cuda.CUDAGraph()
-  with torch.cuda.graph(graph_b, pool=graph.pool()):
-    step(sets[1])
-  graphs = (graph, graph_b)
+  # One graph per buffer set, each with its own memory pool: a graph's
+  # outputs (loss and gradients, read back while the other graph runs) live
+  # in its pool and are rewritten in place by every replay.
+  graphs = []
+  for b in sets:
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+      outs = step(b)
+    b.update(outs)
+    graphs.append(g)
+  graph = graphs[0]
   for _ in range(args.warmup):
     graph.replay()
   torch.cuda.synchronize(device)
@@ -518,8 +514,7 @@ def run_plain(wl, device, args):
       else:
         out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
                                       num_layers=wl.num_layers)
-      _, grads = l2_loss_grads(out, tgt, (v, c))
-      [g * 2.0 for g in grads]
+      l2_loss_grads(out, tgt, (v, c))
 
   for _ in range(2):
     step()

@@ -23,12 +23,14 @@ DR_TEXTURE_PAD_ZERO = 1
 DR_TEXTURE_TEXEL_UNITS = 2
 DR_MAX_IMAGE_DIM = 32768
 DR_STATIC_SCRATCH_BYTES = 64 << 20
+DR_SQUARED_ERROR_PARTIALS = 1216
 
 # Every symbol the header declares, with (restype, argtypes).
 _P = ctypes.c_void_p
 _I = ctypes.c_int32
 _S = ctypes.c_size_t
 _L = ctypes.c_int64
+_F = ctypes.c_float
 
 
 class ImageDesc(ctypes.Structure):
@@ -77,6 +79,7 @@ SIGNATURES = {
     "dr_texture_map_bwd": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P]),
     "dr_composite_over_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_composite_over_bwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P]),
+    "dr_squared_error": (_I, [_P, _P, _L, _F, _P, _P, _P, _P]),
     "dr_vertex_normals_fwd": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "dr_vertex_normals_bwd": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),

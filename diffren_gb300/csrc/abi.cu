@@ -277,6 +277,14 @@ int dr_composite_over_bwd(const float* d_out, const float* shaded, const float* 
                 err);
 }
 
+int dr_squared_error(const float* image, const float* target, int64_t count, float weight,
+                     float* seed, double* partials, float* loss, void* stream) {
+  std::string err;
+  return finish(dr::squared_error_launch(image, target, count, weight, seed, partials, loss,
+                                         as_stream(stream), err),
+                err);
+}
+
 int dr_vertex_normals_fwd(const float* vertices, const int32_t* triangles,
                           const dr_image_desc* meshes, int32_t num_meshes, float* accum,
                           float* normals, void* stream) {

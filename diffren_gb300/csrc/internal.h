@@ -115,6 +115,11 @@ int over_bwd_launch(const float* d_out, const float* shaded, const float* z, int
                     const dr_image_desc* images, int n, int L, float* d_shaded,
                     cudaStream_t stream, std::string& err);
 
+// loss.cu
+int squared_error_launch(const float* image, const float* target, int64_t n, float weight,
+                         float* seed, double* partials, float* loss, cudaStream_t stream,
+                         std::string& err);
+
 // normals.cu
 int normals_fwd_launch(const float* vertices, const int32_t* tris, const dr_image_desc* images,
                        int n, float* accum, float* normals, cudaStream_t stream,

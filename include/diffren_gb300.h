@@ -408,6 +408,20 @@ int dr_splat_jvp(const float* positions, const float* z_buffer, const float* col
                  const dr_image_desc* images, int32_t num_images, int32_t num_layers,
                  float* d_image, void* stream);
 
+/* ------------------------------------------------------------- losses */
+
+/* Beyond the reference interface: the squared-error objective its
+ * optimization tests fit renders with (jnp.mean((image - target)**2),
+ * diffren/jax/internal/splat_test.py:137-167) and its gradient, in one pass:
+ * *loss = weight * sum_i (image_i - target_i)^2 and seed_i = (2 * weight) *
+ * (image_i - target_i), the d_out to seed the renderer's VJP with (weight 1
+ * gives the sum, 1 / count the mean). `partials` is scratch of
+ * DR_SQUARED_ERROR_PARTIALS doubles; `loss` is one float on the device. The
+ * sum order is fixed (deterministic). */
+#define DR_SQUARED_ERROR_PARTIALS 1216
+int dr_squared_error(const float* image, const float* target, int64_t count, float weight,
+                     float* seed, double* partials, float* loss, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,13 +119,29 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
                                    fake, None) == 4
 
 
+def test_squared_error_rejects_bad_arguments():
+  lib = _lib.load()
+  fake = ctypes.c_void_p(256)
+  assert lib.dr_squared_error(fake, fake, -1, 1.0, fake, fake, fake, None) == 1
+  assert lib.dr_squared_error(fake, fake, 4, 1.0, fake, None, fake, None) == 1
+  assert lib.dr_squared_error(None, fake, 4, 1.0, fake, fake, fake, None) == 1
+  assert lib.dr_squared_error(fake, fake, 4, 1.0, fake, fake, None, None) == 1
+
+
+def test_squared_error_takes_cuda_tensors():
+  import torch
+  from diffren_gb300 import losses
+  with pytest.raises(ValueError, match="CUDA tensors"):
+    losses.squared_error_seed(torch.zeros(4), torch.zeros(4))
+
+
 def test_python_constants_match_header():
   with open(HEADER) as f:
     src = f.read()
   for name in ("DR_FLAG_INDEX_OUT_OF_RANGE", "DR_FLAG_NONFINITE_VERTEX", "DR_TEXTURE_PAD_ZERO",
                "DR_TEXTURE_TEXEL_UNITS",
                "DR_MAX_LAYERS", "DR_MAX_CHANNELS", "DR_MAX_BATCH_INLINE", "DR_MAX_IMAGE_DIM",
-               "DR_MAX_SPLAT_CHANNELS", "DR_OK",
+               "DR_MAX_SPLAT_CHANNELS", "DR_OK", "DR_SQUARED_ERROR_PARTIALS",
                "DR_CULL_NONE", "DR_CULL_BACK", "DR_CULL_FRONT", "DR_DEPTH_DISCRETIZED",
                "DR_DEPTH_FLOAT"):
     m = re.search(r"#define %s (\d+)u?" % name, src)
