@@ -65,7 +65,7 @@ def test_optimize_single_triangle(num_components, device):
     if i == 0:
       assert rg is None or float(rg.norm()) == pytest.approx(0.0)
       assert float(sg.norm()) > 0.01
-      initial = float(splat_loss)
+      initial = float(splat_loss.detach())
     var = var - sg
   final = float(((render_splat(var, True) - target) ** 2).mean())
   assert final < 0.5 * initial, (initial, final)
