@@ -893,9 +893,12 @@ __device__ __forceinline__ void sample_adjoint(const Taps& tp, const float4* col
 // color adjoint of class k) and h[k][i] (weight adjoint), next to every
 // layer's depth z[l][i]; each sample of the tile then reads those of the 9
 // pixels it reached, in the class its surface test picked, and writes
-// d color and d viewport xy. No atomics.
+// d color and d viewport xy. No atomics. For up to four channels and three
+// layers the register bound lets five blocks share an SM, the count the
+// shared memory allows (a few bytes of spills, measured faster than four).
 template <int C, int LT>
-__global__ void __launch_bounds__(256, 4) splat_bwd_kernel(SplatArgs a, Batch B) {
+__global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
+    splat_bwd_kernel(SplatArgs a, Batch B) {
   constexpr int Q = Groups<C>::Q;
   extern __shared__ __align__(16) float smem[];
   const TileRef tr = tile_of(B);
