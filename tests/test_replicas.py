@@ -62,3 +62,19 @@ def test_cpu_baseline_loss_equals_autograd_of_the_l2_loss():
   torch.testing.assert_close(l2.detach(), ref.detach(), rtol=1e-6, atol=0)
   gv, gc = torch.autograd.grad(l2, (v, c))
   assert torch.equal(gv, rv) and torch.equal(gc, rc)
+
+
+def test_kernel_bytes_formulas():
+  """The algorithmic bytes behind `roofline.achieved` and `kernels_gbs`:
+  every input read and every output written once, per kernel."""
+  import types
+  wl = types.SimpleNamespace(num_layers=3, pixels=1000, triangles=50, vertices=30)
+  S = 3000
+  b = bench.kernel_bytes(wl, fg=400, near=600, C=4, K=4)
+  assert b["raster"] == 50 * 12 + 30 * 32 + S * 36 + 16 * 400
+  assert b["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 60 * 600
+  assert b["splat_bwd"] == 600 * 76 + 4 * S + 32 * 400 + 16 * S + 16 * 400
+  assert b["samples_bwd"] == 4 * S + 400 * 64 + 30 * 32 * 3
+  assert b["squared_error"] == 48 * 1000
+  # near defaults to every pixel
+  assert bench.kernel_bytes(wl, fg=400)["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 60 * 1000
