@@ -1,7 +1,9 @@
 // Shared device code of the diffren_gb300 kernels: the batch table passed by
 // value in kernel parameters, and the exact triangle arithmetic of diffren's
 // rasterizer written with explicitly rounded intrinsics so that nvcc cannot
-// contract or reorder any float operation.
+// contract or reorder any float operation. Where the reference's CUDA build
+// fuses a multiply and an add (nvcc's default contraction), the discretized
+// depth semantics use an explicit fused multiply-add at that place.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -169,15 +171,22 @@ __device__ __forceinline__ void box_add_point(float x, float y, float w, int W,
 }
 
 // AddNearPoint (rasterize_utils.h:86-99): where edge p0->p1 meets z/w = -1.
+// `fused`: p0 + s (p1 - p0) as one fused multiply-add per coordinate, as
+// nvcc's default contraction compiles it in the reference's CUDA build (the
+// CPU build rounds the product first). The box edge this point sets bounds
+// the visible part of the triangle, so pixels that the two forms' boxes
+// disagree on lie beyond the near plane and never produce a fragment.
 __device__ __forceinline__ void box_add_near(float4 p0, float4 p1, int W, int H,
-                                             int& l, int& r, int& b, int& t) {
+                                             int& l, int& r, int& b, int& t, bool fused) {
   const float denom =
       __fsub_rn(__fadd_rn(__fsub_rn(p0.z, p1.z), p0.w), p1.w);
   if (denom != 0.0f) {
     const float s = __fdiv_rn(__fadd_rn(p0.z, p0.w), denom);
-    const float x = __fadd_rn(p0.x, __fmul_rn(s, __fsub_rn(p1.x, p0.x)));
-    const float y = __fadd_rn(p0.y, __fmul_rn(s, __fsub_rn(p1.y, p0.y)));
-    const float w = __fadd_rn(p0.w, __fmul_rn(s, __fsub_rn(p1.w, p0.w)));
+    const float dx = __fsub_rn(p1.x, p0.x), dy = __fsub_rn(p1.y, p0.y);
+    const float dw = __fsub_rn(p1.w, p0.w);
+    const float x = fused ? __fmaf_rn(s, dx, p0.x) : __fadd_rn(p0.x, __fmul_rn(s, dx));
+    const float y = fused ? __fmaf_rn(s, dy, p0.y) : __fadd_rn(p0.y, __fmul_rn(s, dy));
+    const float w = fused ? __fmaf_rn(s, dw, p0.w) : __fadd_rn(p0.w, __fmul_rn(s, dw));
     box_add_point(x, y, w, W, H, l, r, b, t);
   }
 }
@@ -187,25 +196,25 @@ __device__ __forceinline__ bool clip_visible(float4 p) {
 }
 
 // ComputeTriangleBoundingBox (rasterize_utils.h:111-161). box = {l, r, b, t}
-// with l, b inclusive and r, t exclusive.
+// with l, b inclusive and r, t exclusive. `fused`: see box_add_near.
 __device__ __forceinline__ bool triangle_box(float4 v0, float4 v1, float4 v2,
-                                             int W, int H, int4& box) {
+                                             int W, int H, int4& box, bool fused) {
   int l = W, r = 0, b = H, t = 0;
   const bool s0 = clip_visible(v0), s1 = clip_visible(v1), s2 = clip_visible(v2);
   if (s0) {
     box_add_point(v0.x, v0.y, v0.w, W, H, l, r, b, t);
-    if (!s1) box_add_near(v0, v1, W, H, l, r, b, t);
-    if (!s2) box_add_near(v0, v2, W, H, l, r, b, t);
+    if (!s1) box_add_near(v0, v1, W, H, l, r, b, t, fused);
+    if (!s2) box_add_near(v0, v2, W, H, l, r, b, t, fused);
   }
   if (s1) {
     box_add_point(v1.x, v1.y, v1.w, W, H, l, r, b, t);
-    if (!s2) box_add_near(v1, v2, W, H, l, r, b, t);
-    if (!s0) box_add_near(v1, v0, W, H, l, r, b, t);
+    if (!s2) box_add_near(v1, v2, W, H, l, r, b, t, fused);
+    if (!s0) box_add_near(v1, v0, W, H, l, r, b, t, fused);
   }
   if (s2) {
     box_add_point(v2.x, v2.y, v2.w, W, H, l, r, b, t);
-    if (!s0) box_add_near(v2, v0, W, H, l, r, b, t);
-    if (!s1) box_add_near(v2, v1, W, H, l, r, b, t);
+    if (!s0) box_add_near(v2, v0, W, H, l, r, b, t, fused);
+    if (!s1) box_add_near(v2, v1, W, H, l, r, b, t, fused);
   }
   box = make_int4(l, r, b, t);
   return (r > l) && (t > b);
@@ -240,10 +249,15 @@ __device__ __forceinline__ void edge_matrix(float4 v0, float4 v1, float4 v2,
 }
 
 // Fixed-point NDC coordinate of the center of pixel i of n
-// (rasterize_utils.h:225-228).
-__device__ __forceinline__ long long pixel_center_fixed(int i, int n) {
+// (rasterize_utils.h:225-228). `fused`: (2/n) (i + 0.5) - 1 as one fused
+// multiply-add, which is how nvcc's default contraction compiles the
+// reference's CUDA rasterizer (checked bit for bit against that build); the
+// CPU rasterizer rounds the product first. The two differ only where 2/n is
+// not a power of two.
+__device__ __forceinline__ long long pixel_center_fixed(int i, int n, bool fused) {
   const float scale = __fdiv_rn(2.0f, __int2float_rn(n));
-  const float p = __fsub_rn(__fmul_rn(scale, __fadd_rn(__int2float_rn(i), 0.5f)), 1.0f);
+  const float c = __fadd_rn(__int2float_rn(i), 0.5f);
+  const float p = fused ? __fmaf_rn(scale, c, -1.0f) : __fsub_rn(__fmul_rn(scale, c), 1.0f);
   return to_fixed(p);
 }
 
@@ -268,12 +282,26 @@ __device__ __forceinline__ void barycentrics_of(const long long e[3], float b[3]
   b[2] = __fdiv_rn(__ll2float_rn(e[2]), sum);
 }
 
-// NDC depth of a fragment (rasterize_triangles_impl.cc:87-89).
-__device__ __forceinline__ float fragment_z(const float b[3], float3 vz, float3 vw) {
-  const float cz = __fadd_rn(__fadd_rn(__fmul_rn(b[0], vz.x), __fmul_rn(b[1], vz.y)),
-                             __fmul_rn(b[2], vz.z));
-  const float cw = __fadd_rn(__fadd_rn(__fmul_rn(b[0], vw.x), __fmul_rn(b[1], vw.y)),
-                             __fmul_rn(b[2], vw.z));
+// b0 a0 + b1 a1 + b2 a2 as the reference's CUDA build computes it
+// (rasterize_triangles_impl_cuda.cu.cc:300-302 under nvcc's default
+// contraction, checked bit for bit against that build): the first product
+// fused into the sum with the second, then the third fused in.
+__device__ __forceinline__ float dot3_fused(const float b[3], float a0, float a1, float a2) {
+  return __fmaf_rn(b[2], a2, __fmaf_rn(b[0], a0, __fmul_rn(b[1], a1)));
+}
+
+// The same with every operation rounded, as the CPU rasterizer computes it
+// (rasterize_triangles_impl.cc:87-88).
+__device__ __forceinline__ float dot3_rounded(const float b[3], float a0, float a1, float a2) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(b[0], a0), __fmul_rn(b[1], a1)), __fmul_rn(b[2], a2));
+}
+
+// NDC depth of a fragment (rasterize_triangles_impl.cc:87-89,
+// rasterize_triangles_impl_cuda.cu.cc:300-303); `fused` selects the CUDA
+// build's arithmetic.
+__device__ __forceinline__ float fragment_z(const float b[3], float3 vz, float3 vw, bool fused) {
+  const float cz = fused ? dot3_fused(b, vz.x, vz.y, vz.z) : dot3_rounded(b, vz.x, vz.y, vz.z);
+  const float cw = fused ? dot3_fused(b, vw.x, vw.y, vw.z) : dot3_rounded(b, vw.x, vw.y, vw.z);
   return __fdiv_rn(cz, cw);
 }
 

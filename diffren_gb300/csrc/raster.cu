@@ -98,7 +98,7 @@ Layout make_layout(int64_t tris, int64_t tiles, int images, int large_tiles) {
 // (which are monotone in the pixel index), so it is <= 0 over the whole box
 // iff it is <= 0 at the four corners. Only used when no int64 term can
 // overflow (|m| < 2^43), so the test is exact.
-__device__ bool cannot_cover(const long long m[9], int4 box, int W, int H) {
+__device__ bool cannot_cover(const long long m[9], int4 box, int W, int H, bool fused) {
   const long long lim = 1LL << 43;
 #pragma unroll
   for (int i = 0; i < 9; ++i)
@@ -106,8 +106,10 @@ __device__ bool cannot_cover(const long long m[9], int4 box, int W, int H) {
   const long long A = m[0] + m[3] + m[6];
   const long long B = m[1] + m[4] + m[7];
   const long long C = (m[2] + m[5] + m[8]) * 65536;
-  const long long x0 = pixel_center_fixed(box.x, W), x1 = pixel_center_fixed(box.y - 1, W);
-  const long long y0 = pixel_center_fixed(box.z, H), y1 = pixel_center_fixed(box.w - 1, H);
+  const long long x0 = pixel_center_fixed(box.x, W, fused);
+  const long long x1 = pixel_center_fixed(box.y - 1, W, fused);
+  const long long y0 = pixel_center_fixed(box.z, H, fused);
+  const long long y1 = pixel_center_fixed(box.w - 1, H, fused);
   const long long s00 = A * x0 + B * y0 + C, s10 = A * x1 + B * y0 + C;
   const long long s01 = A * x0 + B * y1 + C, s11 = A * x1 + B * y1 + C;
   return s00 <= 0 && s10 <= 0 && s01 <= 0 && s11 <= 0;
@@ -147,11 +149,12 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
                         (v1.x - v1.x) + (v1.y - v1.y) + (v1.z - v1.z) + (v1.w - v1.w) +
                         (v2.x - v2.x) + (v2.y - v2.y) + (v2.z - v2.z) + (v2.w - v2.w);
     if (probe != 0.0f) atomicOr(&a.counters[1], DR_FLAG_NONFINITE_VERTEX);
-    valid = triangle_box(v0, v1, v2, W, H, box);
+    const bool disc = a.depth_mode == DR_DEPTH_DISCRETIZED;
+    valid = triangle_box(v0, v1, v2, W, H, box, disc);
     if (valid) {
       TriSetup s;
       edge_matrix(v0, v1, v2, a.culling, s.m);
-      valid = !cannot_cover(s.m, box, W, H);
+      valid = !cannot_cover(s.m, box, W, H, disc);
       if (valid) {
         s.vz[0] = v0.z; s.vz[1] = v1.z; s.vz[2] = v2.z;
         s.vw[0] = v0.w; s.vw[1] = v1.w; s.vw[2] = v2.w;
@@ -414,8 +417,8 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
 
     for (int p = threadIdx.x; p < L * TP; p += kThreads) s.keys[p] = kEmpty;
     for (int i = threadIdx.x; i < TW + TH; i += kThreads) {
-      if (i < TW) s.pxf[i] = pixel_center_fixed(x0 + i, W);
-      else s.pyf[i - TW] = pixel_center_fixed(y0 + i - TW, H);
+      if (i < TW) s.pxf[i] = pixel_center_fixed(x0 + i, W, disc);
+      else s.pyf[i - TW] = pixel_center_fixed(y0 + i - TW, H, disc);
     }
     const int nbin = a.tile_count[item];
     const int bin0 = a.tile_first[item];
@@ -498,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
         barycentrics_of(e, b);
         const float3 vz = make_float3(s.vz[j], s.vz[kThreads + j], s.vz[2 * kThreads + j]);
         const float3 vw = make_float3(s.vw[j], s.vw[kThreads + j], s.vw[2 * kThreads + j]);
-        const float z = fragment_z(b, vz, vw);
+        const float z = fragment_z(b, vz, vw, disc);
         unsigned long long key;
         if (disc) {
           if (z < -1.0f || z > 1.0f) continue;  // NaN passes, as in the reference
@@ -587,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
         } else {
           const float3 vz = make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
           const float3 vw = make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
-          zz = fragment_z(bb, vz, vw);
+          zz = fragment_z(bb, vz, vw, false);
         }
         if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
         a.ids[o] = id;
@@ -632,7 +635,7 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
                   make_float3(__ldg(&st->vz[0]), __ldg(&st->vz[1]), __ldg(&st->vz[2]));
               const float3 vw =
                   make_float3(__ldg(&st->vw[0]), __ldg(&st->vw[1]), __ldg(&st->vw[2]));
-              zz = fragment_z(bb, vz, vw);
+              zz = fragment_z(bb, vz, vw, false);
             }
             if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
           }

@@ -1,9 +1,13 @@
-"""Test infrastructure only: ctypes access to the CPU rasterizer checkers.
+"""Test infrastructure only: ctypes access to the rasterizer checkers.
 
 ``rasterize`` runs this repo's C restatement (``raster_oracle.c``);
 ``rasterize_reference_cpu`` runs the reference's own CPU rasterizer
-(``diffren/common/kernels/rasterize_triangles_impl.cc:27-118``) compiled in
-place into ``oracle/_ref`` where the reference tree exists.
+(``diffren/common/kernels/rasterize_triangles_impl.cc:27-118``) and
+``rasterize_reference_cuda`` the reference's own CUDA rasterizer
+(``diffren/common/kernels/rasterize_triangles_impl_cuda.cu.cc:397-484``),
+both compiled by ``oracle/Makefile`` into ``oracle/_ref`` from the reference
+tree (``DIFFREN_REFERENCE`` or an explicit root) or from the git-ignored
+staged copy of its sources in ``oracle/_ref/src``.
 """
 import ctypes
 import os
@@ -14,6 +18,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _ORACLE_SO = os.path.join(_HERE, "_build", "libraster_oracle.so")
 _REF_SO = os.path.join(_HERE, "_ref", "libref_raster.so")
+_REF_CUDA_SO = os.path.join(_HERE, "_ref", "libref_raster_cuda.so")
+_STAGED = os.path.join(_HERE, "_ref", "src")
+_KERNELS = os.path.join("diffren", "common", "kernels")
 
 DEPTH_DISCRETIZED = 0  # reference CUDA rasterizer semantics
 DEPTH_FLOAT = 1  # reference CPU rasterizer semantics
@@ -25,6 +32,7 @@ NAN_TO_I64 = -0x8000000000000000
 
 _lib = None
 _ref = None
+_ref_cuda = None
 
 
 def build(force=False):
@@ -36,15 +44,48 @@ def build(force=False):
   return _ORACLE_SO
 
 
-def build_reference(reference_root="/root/reference"):
-  """Compiles the reference CPU rasterizer in place; None if unavailable."""
-  src = os.path.join(reference_root, "diffren", "common", "kernels",
-                     "rasterize_triangles_impl.cc")
-  if not os.path.exists(src):
+def reference_root(root=None):
+  """The reference tree to build from: `root`, else $DIFFREN_REFERENCE, else
+  None (the staged copy is used when present)."""
+  return root or os.environ.get("DIFFREN_REFERENCE") or None
+
+
+def stage_reference(root=None):
+  """Copies the reference rasterizer sources into oracle/_ref/src
+  (git-ignored), so the reference builds where its tree is absent. Returns
+  False when no reference tree is given."""
+  root = reference_root(root)
+  if root is None or not os.path.exists(os.path.join(root, _KERNELS)):
+    return False
+  subprocess.run(["make", "-s", "-C", _HERE, "stage", "REFERENCE=" + root], check=True)
+  return True
+
+
+def _reference_make(target, source, root):
+  root = reference_root(root)
+  if root is not None and os.path.exists(os.path.join(root, _KERNELS, source)):
+    args = ["REFERENCE=" + root]
+  elif os.path.exists(os.path.join(_STAGED, _KERNELS, source)):
+    args = ["REFERENCE="]
+  else:
+    return False
+  subprocess.run(["make", "-s", "-C", _HERE, target] + args, check=True)
+  return True
+
+
+def build_reference(root=None):
+  """Compiles the reference CPU rasterizer; None if its sources are absent."""
+  if not _reference_make("ref", "rasterize_triangles_impl.cc", root):
     return None
-  subprocess.run(["make", "-s", "-C", _HERE, "ref",
-                  "REFERENCE=" + reference_root], check=True)
   return _REF_SO
+
+
+def build_reference_cuda(root=None):
+  """Compiles the reference CUDA rasterizer for sm_103a with nvcc's default
+  flags; None if its sources are absent."""
+  if not _reference_make("ref_cuda", "rasterize_triangles_impl_cuda.cu.cc", root):
+    return None
+  return _REF_CUDA_SO
 
 
 def _load():
@@ -61,6 +102,10 @@ def reference_available():
   return os.path.exists(_REF_SO)
 
 
+def reference_cuda_available():
+  return os.path.exists(_REF_CUDA_SO)
+
+
 def _load_ref():
   global _ref
   if _ref is None:
@@ -70,6 +115,18 @@ def _load_ref():
     _ref = ctypes.CDLL(_REF_SO)
     _ref.ref_rasterize_cpu.restype = ctypes.c_int
   return _ref
+
+
+def _load_ref_cuda():
+  global _ref_cuda
+  if _ref_cuda is None:
+    if not os.path.exists(_REF_CUDA_SO):
+      raise RuntimeError("reference CUDA rasterizer not built (see oracle/Makefile)")
+    _ref_cuda = ctypes.CDLL(_REF_CUDA_SO)
+    _ref_cuda.ref_rasterize_cuda.restype = ctypes.c_int
+    _ref_cuda.ref_rasterize_cuda.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [
+        ctypes.c_int32] * 5 + [ctypes.c_void_p] * 4 + [ctypes.c_char_p, ctypes.c_int32]
+  return _ref_cuda
 
 
 def _ptr(a):
@@ -115,6 +172,21 @@ def rasterize_reference_cpu(vertices, triangles, width, height, num_layers,
                                 ctypes.c_int32(int(culling)), _ptr(ids), _ptr(z),
                                 _ptr(b))
   return ids, z, b
+
+
+def rasterize_reference_cuda(vertices, triangles, triangle_count, width, height,
+                             num_layers, culling, triangle_ids, z_buffer, barycentrics,
+                             stream=0):
+  """The reference's own CUDA rasterizer on device buffers given as integer
+  addresses (vertices [V,4] f32, triangles [T,3] i32, outputs [L,H,W] i32,
+  [L,H,W] f32, [L,H,W,3] f32), launched on `stream`. Raises on a failed
+  launch. Background samples get id 0 and z 1."""
+  msg = ctypes.create_string_buffer(512)
+  rc = _load_ref_cuda().ref_rasterize_cuda(vertices, triangles, triangle_count, width,
+                                           height, num_layers, int(culling), triangle_ids,
+                                           z_buffer, barycentrics, stream, msg, 512)
+  if rc != 0:
+    raise RuntimeError("reference CUDA rasterizer: " + msg.value.decode())
 
 
 def transform(matrix, vertices):

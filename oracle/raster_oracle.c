@@ -12,6 +12,13 @@
  *       unpack, barycentric recompute)
  * with every float operation written out so that no compiler contraction or
  * platform conversion rule changes a bit (build with -ffp-contract=off).
+ * The reference's CUDA build is compiled by nvcc with its default
+ * contraction, which fuses three multiply-adds of that path: the pixel
+ * centre (2/n)(i + 0.5) - 1, the depth interpolation b0 z0 + b1 z1 + b2 z2
+ * (and w) as fma(b2, z2, fma(b0, z0, b1 z1)), and the near-plane point
+ * p0 + s (p1 - p0). The discretized semantics restate those as explicit
+ * fmaf() calls; outputs of the compiled reference CUDA rasterizer agree bit
+ * for bit with this form and not with the separately rounded one.
  *
  * Two depth semantics, selected by `depth_mode`:
  *   0 (DISCRETIZED): the reference CUDA rasterizer. Per fragment the key is
@@ -85,15 +92,17 @@ static void add_point(float x, float y, float w, int W, int H, int* l, int* r,
   *t = v < 0 ? 0 : (v > H ? H : v);
 }
 
-/* rasterize_utils.h:86-99: intersect edge (p0,p1) with the near plane. */
+/* rasterize_utils.h:86-99: intersect edge (p0,p1) with the near plane;
+ * `fused`: the CUDA build's p0 + s (p1 - p0) as one fma. */
 static void add_near_point(const float* p0, const float* p1, int W, int H,
-                           int* l, int* r, int* b, int* t) {
+                           int* l, int* r, int* b, int* t, int fused) {
   const float denom = ((p0[2] - p1[2]) + p0[3]) - p1[3];
   if (denom != 0.0f) {
     const float s = (p0[2] + p0[3]) / denom;
-    const float x = p0[0] + s * (p1[0] - p0[0]);
-    const float y = p0[1] + s * (p1[1] - p0[1]);
-    const float w = p0[3] + s * (p1[3] - p0[3]);
+    const float dx = p1[0] - p0[0], dy = p1[1] - p0[1], dw = p1[3] - p0[3];
+    const float x = fused ? fmaf(s, dx, p0[0]) : p0[0] + s * dx;
+    const float y = fused ? fmaf(s, dy, p0[1]) : p0[1] + s * dy;
+    const float w = fused ? fmaf(s, dw, p0[3]) : p0[3] + s * dw;
     add_point(x, y, w, W, H, l, r, b, t);
   }
 }
@@ -101,14 +110,14 @@ static void add_near_point(const float* p0, const float* p1, int W, int H,
 static int clip_visible(const float* p) { return p[3] > 0.0f && p[2] >= -p[3]; }
 
 /* rasterize_utils.h:111-161 */
-static int bounding_box(const float* v[3], int W, int H, int box[4]) {
+static int bounding_box(const float* v[3], int W, int H, int box[4], int fused) {
   int l = W, r = 0, b = H, t = 0;
   for (int i = 0; i < 3; ++i) {
     if (!clip_visible(v[i])) continue;
     add_point(v[i][0], v[i][1], v[i][3], W, H, &l, &r, &b, &t);
     const int n1 = (i + 1) % 3, n2 = (i + 2) % 3;
-    if (!clip_visible(v[n1])) add_near_point(v[i], v[n1], W, H, &l, &r, &b, &t);
-    if (!clip_visible(v[n2])) add_near_point(v[i], v[n2], W, H, &l, &r, &b, &t);
+    if (!clip_visible(v[n1])) add_near_point(v[i], v[n1], W, H, &l, &r, &b, &t, fused);
+    if (!clip_visible(v[n2])) add_near_point(v[i], v[n2], W, H, &l, &r, &b, &t, fused);
   }
   box[0] = l;
   box[1] = r;
@@ -142,12 +151,20 @@ static void edge_matrix(const float* v[3], int culling, fx_t m[9]) {
   }
 }
 
-/* rasterize_utils.h:225-228: fixed-point NDC coordinate of pixel center. */
-static fx_t pixel_center_fixed(int i, int n) {
+/* rasterize_utils.h:225-228: fixed-point NDC coordinate of pixel center;
+ * `fused`: the CUDA build's single fma. */
+static fx_t pixel_center_fixed(int i, int n, int fused) {
   const float scale = 2.0f / (float)n;
   const float c = (float)i + 0.5f;
-  const float p = scale * c - 1.0f;
+  const float p = fused ? fmaf(scale, c, -1.0f) : scale * c - 1.0f;
   return to_fixed(p);
+}
+
+/* b0 a0 + b1 a1 + b2 a2: rasterize_triangles_impl.cc:87-88 (rounded), or
+ * rasterize_triangles_impl_cuda.cu.cc:300-301 as the CUDA build fuses it. */
+static float dot3(const float b[3], float a0, float a1, float a2, int fused) {
+  if (fused) return fmaf(b[2], a2, fmaf(b[0], a0, b[1] * a1));
+  return (b[0] * a0 + b[1] * a1) + b[2] * a2;
 }
 
 typedef struct {
@@ -158,7 +175,7 @@ typedef struct {
 
 /* rasterize_utils.h:220-248 and rasterize_triangles_impl.cc:79-89 */
 static void shade_fragment(const fx_t m[9], fx_t px, fx_t py, const float* v[3],
-                           fragment_t* f) {
+                           int fused, fragment_t* f) {
   fx_t e[3];
   for (int i = 0; i < 3; ++i)
     e[i] = wadd(wadd(wmul(m[3 * i], px), wmul(m[3 * i + 1], py)), wshl16(m[3 * i + 2]));
@@ -166,8 +183,8 @@ static void shade_fragment(const fx_t m[9], fx_t px, fx_t py, const float* v[3],
   if (!f->inside) return;
   const float sum = (float)wadd(wadd(e[0], e[1]), e[2]);
   for (int i = 0; i < 3; ++i) f->b[i] = (float)e[i] / sum;
-  const float cz = (f->b[0] * v[0][2] + f->b[1] * v[1][2]) + f->b[2] * v[2][2];
-  const float cw = (f->b[0] * v[0][3] + f->b[1] * v[1][3]) + f->b[2] * v[2][3];
+  const float cz = dot3(f->b, v[0][2], v[1][2], v[2][2], fused);
+  const float cw = dot3(f->b, v[0][3], v[1][3], v[2][3], fused);
   f->z = cz / cw;
 }
 
@@ -200,6 +217,7 @@ int oracle_rasterize(const float* verts, const int32_t* tris, int32_t T,
   const int64_t npix = (int64_t)W * H;
   uint64_t* keys = (uint64_t*)malloc(sizeof(uint64_t) * npix * L);
   if (!keys) return -1;
+  const int fused = depth_mode == kDepthDiscretized;
   const uint64_t empty = (depth_mode == kDepthDiscretized)
                              ? ((uint64_t)discretize_z(1.0f) << 32)
                              : ((uint64_t)float_order_bits(1.0f) << 32);
@@ -209,14 +227,14 @@ int oracle_rasterize(const float* verts, const int32_t* tris, int32_t T,
     const float* v[3] = {vertex_ptr(verts, tris, t, 0), vertex_ptr(verts, tris, t, 1),
                          vertex_ptr(verts, tris, t, 2)};
     int box[4];
-    if (!bounding_box(v, W, H, box)) continue;
+    if (!bounding_box(v, W, H, box, fused)) continue;
     fx_t m[9];
     edge_matrix(v, culling, m);
     for (int iy = box[2]; iy < box[3]; ++iy) {
-      const fx_t py = pixel_center_fixed(iy, H);
+      const fx_t py = pixel_center_fixed(iy, H, fused);
       for (int ix = box[0]; ix < box[1]; ++ix) {
         fragment_t f;
-        shade_fragment(m, pixel_center_fixed(ix, W), py, v, &f);
+        shade_fragment(m, pixel_center_fixed(ix, W, fused), py, v, fused, &f);
         if (!f.inside) continue;
         if (f.z < -1.0f || f.z > 1.0f) continue;
         uint64_t key;
@@ -259,7 +277,8 @@ int oracle_rasterize(const float* verts, const int32_t* tris, int32_t T,
         fx_t m[9];
         edge_matrix(v, culling, m);
         fragment_t f;
-        shade_fragment(m, pixel_center_fixed(ix, W), pixel_center_fixed(iy, H), v, &f);
+        shade_fragment(m, pixel_center_fixed(ix, W, fused), pixel_center_fixed(iy, H, fused), v,
+                       fused, &f);
         if (depth_mode == kDepthDiscretized) {
           /* Unpack (cu.cc:178-183), then barycentrics only where z != 1
            * (cu.cc:381-394); the recompute skips the inside test. */

@@ -1,16 +1,18 @@
 """Generates the committed golden fixtures of tests/golden from the reference.
 
 Run where the reference tree exists (it is read-only input):
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <diffren source tree>
+(or with DIFFREN_REFERENCE set to that tree).
 
 It (1) compiles the reference's own CPU rasterizer in place
 (oracle/Makefile `ref`) and records its outputs on seeded and reference-test
 geometry (raster_ref.npz); (2) extracts the reference tests' fixtures and
 known answers from their source text (cube vertices, triangle cases, the
 differentiable-barycentrics Jacobian of rasterize_test.py:216-224); (3)
-decodes the small golden PNGs the GPU tests compare against, and (4) keeps
+decodes the small golden PNGs the GPU tests compare against, (4) keeps
 the textured spot mesh, its texture and its blurred target render
-(spot.npz). Nothing here is used at run time by the library.
+(spot.npz), and (5) keeps the file bytes of the rasterizer's golden PNGs
+(raster_pngs.npz) that the oracle tests decode. Nothing here is used at run time by the library.
 """
 import argparse
 import ast
@@ -128,11 +130,19 @@ def bilinear_boundary_cases(path):
           "shape": np.array([30, 10], np.int32)}
 
 
+RASTER_PNGS = ["Simple_Triangle.png", "External_Triangle.png", "Simple_Tetrahedron.png",
+               "Inside_Box.png", "Ids_Cube.png", "Ids_Cube_Back.png", "Barycentrics_Cube.png",
+               "Barycentrics_Cube_Back.png", "UV_Sphere_Ids.png"]
+
+
 def main():
   ap = argparse.ArgumentParser()
-  ap.add_argument("--reference", default="/root/reference")
+  ap.add_argument("--reference", default=os.environ.get("DIFFREN_REFERENCE"),
+                  help="root of the diffren source tree (default $DIFFREN_REFERENCE)")
   args = ap.parse_args()
   ref = args.reference
+  if not ref:
+    raise SystemExit("pass --reference or set DIFFREN_REFERENCE")
   kern = os.path.join(ref, "diffren", "common", "kernels")
   data = os.path.join(ref, "diffren", "common", "test_data")
   if raster.build_reference(ref) is None:
@@ -229,6 +239,12 @@ def main():
                       point=png.read_png(os.path.join(data, "Spot_Textured_Pt_Light.png")),
                       phong_point=png.read_png(
                           os.path.join(data, "Spot_Textured_Phong_Point.png")))
+
+  # The rasterizer goldens of rasterize_triangles_impl_test.cc and
+  # rasterize_triangles_impl_cuda_test.cc, as their PNG file bytes.
+  np.savez_compressed(os.path.join(HERE, "raster_pngs.npz"), **{
+      name[:-4]: np.frombuffer(open(os.path.join(data, name), "rb").read(), np.uint8)
+      for name in RASTER_PNGS})
 
   # Bilinear resampling known answers (image_test.py boundary cases).
   np.savez_compressed(os.path.join(HERE, "texture_cases.npz"),

@@ -20,9 +20,14 @@ def _paeth_row(line, prev, bpp):
 
 
 def read_png(path):
-  data = open(path, "rb").read()
+  return decode_png(open(path, "rb").read(), path)
+
+
+def decode_png(data, name="<bytes>"):
+  """Decodes the bytes of a PNG file (bytes or a uint8 array)."""
+  data = bytes(np.asarray(bytearray(data) if isinstance(data, bytes) else data, np.uint8))
   if data[:8] != b"\x89PNG\r\n\x1a\n":
-    raise ValueError("not a PNG: %s" % path)
+    raise ValueError("not a PNG: %s" % name)
   pos, idat = 8, b""
   while pos < len(data):
     (n,) = struct.unpack(">I", data[pos:pos + 4])

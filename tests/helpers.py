@@ -7,8 +7,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-REFERENCE = "/root/reference"
-REF_TEST_DATA = os.path.join(REFERENCE, "diffren", "common", "test_data")
+# The diffren source tree, where a test wants it (only the fixture generator
+# and the reference builds read it; set DIFFREN_REFERENCE to use it).
+REFERENCE = os.environ.get("DIFFREN_REFERENCE", "")
 
 IMAGE_WIDTH = 640
 IMAGE_HEIGHT = 480
@@ -16,10 +17,6 @@ IMAGE_HEIGHT = 480
 
 def golden(name):
   return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
-
-
-def reference_data_available():
-  return os.path.isdir(REF_TEST_DATA)
 
 
 # diffren/common/test_utils.py:38-96

@@ -39,27 +39,67 @@ def test_oracle_float_mode_matches_reference_fixture(name):
 
 @pytest.mark.parametrize("name", CASES)
 def test_discretized_mode_agrees_with_float_mode(name):
-  """Reference CUDA vs CPU semantics: same visible triangles except at
-  background (id 0 vs -1) and depth near-ties (< 2 depth quanta)."""
+  """Reference CUDA vs CPU semantics: the same visible triangles except at
+  background (id 0 vs -1), depth near-ties and a few edge pixels. The CUDA
+  build fuses the pixel-centre multiply-add, which moves a pixel centre by
+  at most one 16.16 fixed-point step (2^-16 in NDC) where the width is not
+  a power of two: coverage can change at triangle edges, and barycentrics
+  and depth agree to that step times their gradient (closely on most
+  samples, loosely on small triangles). Each semantics is pinned bit for bit
+  against its own reference build elsewhere."""
   v, t, w, h, layers, cull, ids, z, bary = _case(name)
   gi, gz, gb = raster.rasterize(v, t, w, h, layers, cull, raster.DEPTH_DISCRETIZED)
   fg = ids >= 0
-  np.testing.assert_array_equal(gi[~fg], 0)
-  np.testing.assert_array_equal(gz[~fg], 1.0)
-  diff = fg & (gi != ids)
-  # Near ties: the float depths of the two candidates are within 2 quanta.
-  assert diff.sum() <= max(2, 0.001 * fg.sum()), diff.sum()
-  same = fg & (gi == ids)
-  np.testing.assert_allclose(gz[same], z[same], atol=2.0 / 2147483647.0 * 2, rtol=0)
-  np.testing.assert_array_equal(_bits(gb[same]), _bits(bary[same]))
+  gfg = gz != 1.0
+  np.testing.assert_array_equal(gi[~gfg], 0)
+  np.testing.assert_array_equal(gz[~gfg], 1.0)
+  limit = max(2, 0.002 * fg.sum())
+  assert (gfg != fg).sum() <= limit, (gfg != fg).sum()
+  both = fg & gfg
+  assert (both & (gi != ids)).sum() <= limit, (both & (gi != ids)).sum()
+  same = both & (gi == ids)
+  for a, b in ((gz[same], z[same]), (gb[same], bary[same])):
+    d = np.abs(a - b)
+    if d.size == 0:
+      continue
+    assert d.max() < 2e-2, d.max()
+    assert np.median(d) < 1e-5, np.median(d)
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(
-    helpers.REFERENCE, "diffren/common/kernels/rasterize_triangles_impl.cc")),
-                    reason="reference tree not present")
+CUDA_FIX = helpers.golden("raster_ref_cuda.npz")
+CUDA_CASES = sorted({k.split("__")[0] for k in CUDA_FIX.files})
+
+
+def _cuda_case(name):
+  """Inputs of a recorded reference-CUDA case: a raster_ref.npz scene or a
+  seeded scene named by tests/golden/make_golden_cuda.py."""
+  g = lambda k: CUDA_FIX[name + "__" + k]
+  w, h, layers, cull = (int(x) for x in g("meta"))
+  if name in CASES:
+    v, t = FIX[name + "__vertices"], FIX[name + "__triangles"]
+  else:
+    from golden import make_golden_cuda
+    v, t = make_golden_cuda.seeded_scene(name, w, h)
+  return v, t, w, h, layers, cull, g("ids"), g("z"), g("bary")
+
+
+@pytest.mark.parametrize("name", CUDA_CASES)
+def test_discretized_mode_matches_reference_cuda_fixture(name):
+  """The discretized semantics against outputs recorded from the reference's
+  own CUDA rasterizer (rasterize_triangles_impl_cuda.cu.cc, built for sm_103a
+  with nvcc's defaults): bit-exact ids, depth and barycentrics."""
+  v, t, w, h, layers, cull, ids, z, bary = _cuda_case(name)
+  oi, oz, ob = raster.rasterize(v, t, w, h, layers, cull, raster.DEPTH_DISCRETIZED)
+  np.testing.assert_array_equal(oi, ids)
+  np.testing.assert_array_equal(_bits(oz), _bits(z))
+  np.testing.assert_array_equal(_bits(ob), _bits(bary))
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_oracle_matches_compiled_reference_random(seed):
-  raster.build_reference(helpers.REFERENCE)
+  if raster.build_reference() is None:
+    pytest.skip("reference rasterizer sources not present (DIFFREN_REFERENCE or the "
+                "staged copy in oracle/_ref/src)")
   rng = np.random.default_rng(100 + seed)
   w, h = int(rng.integers(1, 90)), int(rng.integers(1, 70))
   layers, cull = int(rng.integers(1, 6)), int(rng.integers(0, 3))
@@ -73,19 +113,18 @@ def test_oracle_matches_compiled_reference_random(seed):
                                   np.asarray(b).view(np.uint32))
 
 
-needs_ref_data = pytest.mark.skipif(not helpers.reference_data_available(),
-                                    reason="reference test data not present")
+PNGS = helpers.golden("raster_pngs.npz")
 
 
 def _ref_png(name):
-  return png.read_png(os.path.join(helpers.REF_TEST_DATA, name))
+  """A golden PNG of the reference's rasterizer tests (kept as file bytes)."""
+  return png.decode_png(PNGS[name[:-4]], name)
 
 
 def _test_case(name):
   return _case("test_" + name)[:2]
 
 
-@needs_ref_data
 @pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
 @pytest.mark.parametrize("case,golden", [
     ("CanRasterizeTriangle", "Simple_Triangle.png"),
@@ -100,7 +139,6 @@ def test_oracle_golden_barycentrics(case, golden, mode):
   assert ok, msg
 
 
-@needs_ref_data
 @pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
 def test_oracle_golden_inside_box(mode):
   v = FIX["inside_box__vertices"]
@@ -111,7 +149,6 @@ def test_oracle_golden_inside_box(mode):
   assert ok, msg
 
 
-@needs_ref_data
 @pytest.mark.parametrize("mode", [raster.DEPTH_FLOAT, raster.DEPTH_DISCRETIZED])
 def test_oracle_golden_cube_two_layers_and_culling(mode):
   """impl_test.cc:227-294: ids and barycentrics of both layers; culling."""
@@ -136,7 +173,6 @@ def test_oracle_golden_cube_two_layers_and_culling(mode):
     assert (ids[1] == empty).all()
 
 
-@needs_ref_data
 def test_oracle_golden_uv_sphere_ids():
   """rasterize_triangles_impl_cuda_test.cc:172-187 (CUDA semantics)."""
   v, t = helpers.uv_sphere(230, 230, 0.9)
