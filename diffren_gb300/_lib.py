@@ -61,6 +61,7 @@ SIGNATURES = {
     "dr_rasterize_triangles_static_scratch": (_I, [_P, _I, _P, _I, _I, _I, _I, _I,
                                                    _I, _P, _P, _P, _P]),
     "dr_read_error_flags": (_I, [_P, _P, _P]),
+    "dr_read_static_scratch_error_flags": (_I, [_P, _P]),
     "dr_selftest_depth_codec": (_I, [_P, _P]),
     "dr_transform_vertices": (_I, [_P, _P, _I, _P, _I, _P, _P]),
     "dr_transform_vertices_bwd": (_I, [_P, _P, _I, _P, _I, _P, _P]),

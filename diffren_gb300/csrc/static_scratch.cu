@@ -10,12 +10,23 @@
 // position. For them, dr_rasterize_triangles_static_scratch keeps the
 // scratch in a device array that is part of this library's module image.
 //
-// The array has a fixed size, DR_STATIC_SCRATCH_BYTES, and every GPU that
-// loads the library holds it until the process exits. Every call shares it
-// and it keeps the previous call's contents; the rasterizer clears the part
-// that must start at zero on each call. Calls whose work overlaps on the GPU
-// (on different streams, or from different threads) race on the array: the
-// caller must order them, e.g. by issuing them on one stream.
+// The array has a fixed size, DR_STATIC_SCRATCH_BYTES. A device takes it
+// when this library's module is loaded in that device's context: under
+// CUDA's default lazy loading that is the first static-scratch call on the
+// device (the address lookup below loads the module), with
+// CUDA_MODULE_LOADING=EAGER it is context creation. It is held until the
+// context ends (process exit). Every call shares it and it keeps the
+// previous call's contents; the rasterizer clears the part that must start
+// at zero on each call. Calls whose work overlaps on the GPU (on different
+// streams, or from different threads) race on the array: the caller must
+// order them, e.g. by issuing them on one stream.
+//
+// The device address of the array belongs to a CUDA context. It is looked
+// up once per (device, context) pair, with that device current, and cached;
+// a new context on the device (after cudaDeviceReset, or a driver-API
+// context made current by the caller) gets its own lookup.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -30,11 +41,39 @@ __device__ __align__(256) unsigned char g_static_scratch[DR_STATIC_SCRATCH_BYTES
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices] = {};
+struct CachedAddress {
+  CUcontext context;
+  void* address;
+};
+CachedAddress g_scratch_address[kMaxDevices] = {};
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
 
-// Device address of g_static_scratch on the current device. The host-side
-// name of the array is only a stand-in; its device address must be queried
-// once per device, with that device current.
+// The current CUDA context (null if none is bound yet), through the driver
+// entry point the runtime hands out (no link against libcuda).
+int current_context(CUcontext* ctx, std::string& err) {
+  if (g_ctx_get_current == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000,
+                                                           cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || fn == nullptr) {
+      err = "cuCtxGetCurrent is not available from the CUDA runtime";
+      return DR_ERR_CUDA;
+    }
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+  }
+  *ctx = nullptr;
+  if (g_ctx_get_current(ctx) != CUDA_SUCCESS) {
+    err = "cuCtxGetCurrent failed";
+    return DR_ERR_CUDA;
+  }
+  return DR_OK;
+}
+
+// Device address of g_static_scratch in the current context. The host-side
+// name of the array is only a stand-in; its device address is queried with
+// the device current, once per (device, context).
 int scratch_address(void** out, std::string& err) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -47,16 +86,25 @@ int scratch_address(void** out, std::string& err) {
     return DR_ERR_INVALID_ARGUMENT;
   }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_address[dev] == nullptr) {
+  CUcontext ctx = nullptr;
+  int rc = current_context(&ctx, err);
+  if (rc != DR_OK) return rc;
+  CachedAddress& c = g_scratch_address[dev];
+  if (ctx == nullptr || c.address == nullptr || c.context != ctx) {
+    // The lookup binds the device's primary context when none is current
+    // yet, and loads this library's module in it (which takes the array).
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess || p == nullptr) {
       err = std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e);
       return DR_ERR_CUDA;
     }
-    g_scratch_address[dev] = p;
+    rc = current_context(&ctx, err);
+    if (rc != DR_OK) return rc;
+    c.context = ctx;
+    c.address = p;
   }
-  *out = g_scratch_address[dev];
+  *out = c.address;
   return DR_OK;
 }
 
@@ -103,4 +151,21 @@ extern "C" int dr_rasterize_triangles_static_scratch(
                            reinterpret_cast<cudaStream_t>(stream), err);
   if (rc != DR_OK) dr::set_last_error(err);
   return rc;
+}
+
+extern "C" int dr_read_static_scratch_error_flags(uint32_t* flags, void* stream) {
+  std::string err;
+  int rc = DR_OK;
+  if (flags == nullptr) {
+    err = "flags must be non-null";
+    rc = DR_ERR_INVALID_ARGUMENT;
+  }
+  void* scratch = nullptr;
+  if (rc == DR_OK) rc = scratch_address(&scratch, err);
+  if (rc != DR_OK) {
+    dr::set_last_error(err);
+    return rc;
+  }
+  // Same word and same read as dr_read_error_flags on a caller workspace.
+  return dr_read_error_flags(scratch, flags, stream);
 }

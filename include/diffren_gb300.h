@@ -172,19 +172,28 @@ int dr_rasterize_triangles(const float* vertices, int32_t num_vertices,
  * reference). It is for callers that cannot allocate device memory for
  * scratch space, such as an XLA custom-call handler, which gets only its
  * input and result buffers from XLA. The scratch lives in a static device
- * array of DR_STATIC_SCRATCH_BYTES inside this library, which every GPU that
- * loads the library holds until exit; requests that need more return
- * DR_ERR_WORKSPACE_TOO_SMALL without running anything. The first call on a
- * device looks up the array's device address (once per device, with that
- * device current); make that first call before any stream capture. All
- * calls share the array, so calls that overlap on the GPU race: order them
- * (e.g. one stream). The call itself allocates nothing. */
+ * array of DR_STATIC_SCRATCH_BYTES inside this library; requests that need
+ * more return DR_ERR_WORKSPACE_TOO_SMALL without running anything. A device
+ * takes the array's memory when the library's module loads in its context:
+ * under CUDA's default lazy loading at the first static-scratch call on that
+ * device, with CUDA_MODULE_LOADING=EAGER at context creation; it is held
+ * until the process exits. The first call on a device (and in each new
+ * context on it) looks up the array's device address with that device
+ * current; make that first call before any stream capture. All calls share
+ * the array, so calls that overlap on the GPU race: order them (e.g. one
+ * stream). The call itself allocates nothing. */
 #define DR_STATIC_SCRATCH_BYTES (64u << 20)
 int dr_rasterize_triangles_static_scratch(
     const float* vertices, int32_t num_vertices, const int32_t* triangles,
     int32_t num_triangles, int32_t image_width, int32_t image_height,
     int32_t num_layers, int32_t face_culling_mode, int32_t depth_mode,
     int32_t* triangle_ids, float* z_buffer, float* barycentrics, void* stream);
+
+/* dr_read_error_flags for dr_rasterize_triangles_static_scratch, whose
+ * caller never sees the scratch array: synchronizes `stream` and reads the
+ * DR_FLAG_* bits of the last static-scratch call on the current device. No
+ * counterpart in the reference (it does not check indices). */
+int dr_read_static_scratch_error_flags(uint32_t* flags, void* stream);
 
 /* Synchronizes `stream` and reads the device error word of the last raster
  * call that used `workspace` (DR_FLAG_* bits). */
