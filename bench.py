@@ -18,12 +18,16 @@ Reported (one JSON line on rank 0):
              inputs copied in and loss + gradients copied out every step.
   roofline   dominant kernel: algorithmic bytes / CUDA-event duration vs the
              measured HBM copy bandwidth.
-  cpu_baseline  the CPU port of the reference path (C restatement of the
-             reference CPU rasterizer + torch CPU restatement of the JAX
-             interpolate/splat/composite and its autodiff), on a sample.
+  cpu_baseline  the reference path on the host cores, on a sample of the
+             workload: the reference's own C++ CPU rasterizer (built from
+             the reference sources by oracle/Makefile) + the torch CPU
+             restatement of the JAX interpolate/splat/composite and its
+             autodiff (JAX is not installed).
+  parity     the first images of the benchmarked step and their vertex and
+             color gradients against the CPU path in the same depth
+             semantics (1e-5 rel / 1e-6 abs images, 1e-4 gradients).
 
-`--impl reference` times that CPU port alone (the reference's own CPU code
-cannot be built on the GPU host: its sources are not there).
+`--impl reference` times that CPU path alone, one image per step.
 Multi-GPU: replicas only (each rank renders the full batch independently).
 """
 import argparse
@@ -53,6 +57,8 @@ def parse():
   ap.add_argument("--num-meshes", type=int, default=64)
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--no-plain", action="store_true")
+  ap.add_argument("--no-parity", action="store_true",
+                  help="skip the CPU comparison of the first images and gradients")
   ap.add_argument("--cpu-budget", type=float, default=20.0,
                   help="seconds of CPU work per reference-arm step / baseline")
   return ap.parse_args()
@@ -356,7 +362,7 @@ def run_ours(args, rank, world, device):
     else:
       out = r.render(v, {"rgba": rgba(c)}, cams, shader)
     loss, (gv, gc) = l2_loss_grads(out, target, (v, c))
-    return dict(g_v=gv, g_c=gc.contiguous(), loss=loss)
+    return dict(g_v=gv, g_c=gc.contiguous(), loss=loss, out=out.detach())
 
   # Eager warm-up on a side stream, then capture the step.
   s = torch.cuda.Stream(device)
@@ -365,11 +371,21 @@ def run_ours(args, rank, world, device):
     for _ in range(max(args.warmup, 3)):
       step()
   torch.cuda.current_stream(device).wait_stream(s)
-  # Launch count of our kernels in one step (eager).
+  # Launch count of our kernels in one step (eager), and the step's results
+  # on the first images for the parity check.
   kernels.LAUNCHES.reset()
-  step()
+  res0 = step()
   torch.cuda.synchronize(device)
   launches_per_step = kernels.LAUNCHES.count
+  gpu = None
+  if rank == 0 and not args.no_parity:
+    nck = min(16, r.batch.n)
+    vo = np.cumsum([0] + [len(m.vertices) for m in wl.meshes])
+    gpu = {"images": [x.cpu().numpy() for x in r.images(res0["out"])[:nck]],
+           "g_v": [res0["g_v"][vo[i]:vo[i + 1]].cpu().numpy() for i in range(nck)],
+           "g_c": [None if textured else res0["g_c"][vo[i]:vo[i + 1]].cpu().numpy()
+                   for i in range(nck)]}
+  del res0
   # Foreground layer samples of the workload, and pixels within one pixel
   # of one (for the algorithmic bytes).
   with torch.no_grad():
@@ -480,7 +496,7 @@ def run_ours(args, rank, world, device):
   tile = [r.config.tile_width, r.config.tile_height, r.config.large_tiles]
   return dict(wl=wl, fg=fg, near=near, tile=tile, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
               loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
-              plain=plain, renderer=r)
+              plain=plain, renderer=r, gpu=gpu)
 
 
 def run_plain(wl, device, args):
@@ -519,7 +535,7 @@ def run_plain(wl, device, args):
   for _ in range(2):
     step()
   torch.cuda.synchronize(device)
-  k = max(1, min(args.steps, 3))
+  k = max(10, min(args.steps, 20))
   e0 = torch.cuda.Event(enable_timing=True)
   e1 = torch.cuda.Event(enable_timing=True)
   e0.record()
@@ -532,99 +548,175 @@ def run_plain(wl, device, args):
 
 
 # -------------------------------------------------------- CPU (reference)
-def cpu_port_sample(wl, budget_s, threads, images=None):
-  """Times the CPU port on images of the workload until `budget_s` of work
-  (or on exactly the given `images`).
+def cpu_rasterize(wl, i, kind):
+  """Clip vertices and (ids, z, bary) of image i on the CPU. kind
+  "reference": the reference's own C++ CPU rasterizer
+  (rasterize_triangles_impl.cc:27-118, compiled by oracle/Makefile; float
+  depth, single-threaded per image, as the reference runs it); "oracle": the
+  C restatement in the discretized semantics of the reference's CUDA
+  rasterizer, which the GPU path computes (checked bit for bit against the
+  reference's CUDA build by the tests)."""
+  from oracle import raster
+  m, cam, (w, h) = wl.meshes[i], wl.cams[i], wl.sizes[i]
+  clip = raster.transform(cam, m.vertices)
+  if kind == "reference":
+    return clip, raster.rasterize_reference_cpu(clip, m.triangles, w, h, wl.num_layers, 1)
+  return clip, raster.rasterize(clip, m.triangles, w, h, wl.num_layers, 1,
+                                raster.DEPTH_DISCRETIZED)
 
-  Rasterization: the C restatement of the reference CPU rasterizer (float
-  depth semantics, single-threaded per image like the reference's), a group
-  of `threads` images at a time on `threads` host threads. Interpolate,
-  shade, splat, normalize, composite, L2 loss and the backward: the torch CPU
-  float32 restatement of the reference's JAX code with torch autograd, on
-  `threads` threads. Returns (pixels, seconds, images used).
-  """
-  import concurrent.futures
+
+def cpu_render(wl, i, clip, rast, ttex=None):
+  """Interpolate, shade, splat, normalize, composite, L2 loss and the
+  backward of image i on the CPU: the torch float32 restatement of the
+  reference's JAX code (oracle/torch_ref.py) with torch autograd standing in
+  for jax.grad. The forward uses the exact clip vertices the rasterizer saw;
+  gradients flow to the world vertices through the camera matrix. Returns
+  (image [H, W, C], d vertices [V, 3], d colors [V, 3] or None)."""
   import torch
   from oracle import mesh as omesh
-  from oracle import raster, texture, torch_ref
+  from oracle import texture, torch_ref
+  ids, z, b = rast
+  m, (w, h), tgt = wl.meshes[i], wl.sizes[i], wl.targets[i]
+  state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
+  ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
+  tv = torch.tensor(m.vertices, requires_grad=True)
+  cam = torch.tensor(wl.cams[i], dtype=torch.float32)
+  lin = torch.cat([tv, torch.ones_like(tv[:, :1])], 1) @ cam.T
+  tc = torch.tensor(clip) + (lin - lin.detach())  # exact values, camera gradient
+  tparam = None
+  if ttex is not None:
+    uvs = torch_ref.interpolate(torch.tensor(m.uvs), ti, tz, tb, tt)
+    shaded = texture.texture_map_t(uvs, ttex)
+  elif wl.lit:
+    tparam = torch.tensor(m.colors, requires_grad=True)
+    attrs = torch.cat([tparam, omesh.vertex_normals_t(tv, tt), tv], 1)
+    a = torch_ref.interpolate(attrs, ti, tz, tb, tt)
+    shaded = lit_shader({"rgb": a[..., :3], "normals": a[..., 3:6], "pos": a[..., 6:9]})
+  else:
+    tparam = torch.tensor(m.colors, requires_grad=True)
+    shaded = torch_ref.interpolate(rgba(tparam), ti, tz, tb, tt)
+  out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
+  loss = l2_loss(out, torch.tensor(tgt))
+  params = [tv] + ([tparam] if tparam is not None else []) + (
+      [ttex] if ttex is not None else [])
+  grads = torch.autograd.grad(loss, params)
+  return (out.detach().numpy(), grads[0].numpy(),
+          grads[1].numpy() if tparam is not None else None)
+
+
+def cpu_port_sample(wl, budget_s, threads, images=None, kind="reference", keep=False):
+  """Times the CPU path on images of the workload until `budget_s` of work
+  (or on exactly the given `images`): rasterization (`cpu_rasterize`), a
+  group of `threads` images at a time on `threads` host threads, then
+  `cpu_render` of each on `threads` torch threads. Returns (pixels, seconds,
+  images used, {image: (image, d vertices, d colors)} if keep)."""
+  import concurrent.futures
+  import torch
   torch.set_num_threads(threads)
   ttex = None if wl.texture is None else torch.tensor(wl.texture, requires_grad=True)
   order = list(images) if images is not None else list(range(len(wl.meshes)))
-
-  def rasterize(i):
-    m, cam, (w, h) = wl.meshes[i], wl.cams[i], wl.sizes[i]
-    clip = raster.transform(cam, m.vertices)
-    return clip, raster.rasterize(clip, m.triangles, w, h, wl.num_layers, 1,
-                                  raster.DEPTH_FLOAT)
-
   px = used = 0
   t_total = 0.0
+  kept = {}
   with concurrent.futures.ThreadPoolExecutor(threads) as pool:
     for g0 in range(0, len(order), threads):
       group = order[g0:g0 + threads]
       t0 = time.perf_counter()
-      rasters = list(pool.map(rasterize, group))  # ctypes calls release the GIL
-      for i, (clip, (ids, z, b)) in zip(group, rasters):
-        m, (w, h), tgt = wl.meshes[i], wl.sizes[i], wl.targets[i]
-        state = torch_ref.discrete_state(clip, ids, z, b, m.triangles, w, h)
-        tc = torch.tensor(clip, requires_grad=True)
-        ti, tz, tb, tt = (torch.tensor(x) for x in (ids, z, b, m.triangles))
-        tv = tc
-        if wl.lit:
-          # Clip vertices from world vertices in torch, so that the
-          # gradient reaches the vertices through the normals too.
-          tv = torch.tensor(m.vertices, requires_grad=True)
-          cam = torch.tensor(wl.cams[i], dtype=torch.float32)
-          tc = torch.cat([tv, torch.ones_like(tv[:, :1])], 1) @ cam.T
-        if ttex is not None:
-          tparam = ttex
-          uvs = torch_ref.interpolate(torch.tensor(m.uvs), ti, tz, tb, tt)
-          shaded = texture.texture_map_t(uvs, ttex)
-        elif wl.lit:
-          tparam = torch.tensor(m.colors, requires_grad=True)
-          attrs = torch.cat([tparam, omesh.vertex_normals_t(tv, tt), tv], 1)
-          a = torch_ref.interpolate(attrs, ti, tz, tb, tt)
-          shaded = lit_shader({"rgb": a[..., :3], "normals": a[..., 3:6], "pos": a[..., 6:9]})
-        else:
-          tparam = torch.tensor(m.colors, requires_grad=True)
-          shaded = torch_ref.interpolate(rgba(tparam), ti, tz, tb, tt)
-        out = torch_ref.splat_shaded_pixels(tc, ti, tz, tb, tt, shaded, w, h, state)[0]
-        loss = l2_loss(out, torch.tensor(tgt))
-        torch.autograd.grad(loss, (tv, tparam))
-        px += w * h
+      # ctypes calls release the GIL: the rasterizers run in parallel.
+      rasters = list(pool.map(lambda i: cpu_rasterize(wl, i, kind), group))
+      for i, (clip, rast) in zip(group, rasters):
+        res = cpu_render(wl, i, clip, rast, ttex)
+        if keep:
+          kept[i] = res
+        px += wl.sizes[i][0] * wl.sizes[i][1]
         used += 1
       t_total += time.perf_counter() - t0
       if images is None and t_total >= budget_s:
         break
-  return px, t_total, used
+  return px, t_total, used, kept
+
+
+def parity_check(wl, gpu, budget_s, threads):
+  """Compares the benchmarked GPU step with the CPU path on the first images
+  of the workload (until `budget_s` of CPU work, at most 16 images): the
+  rasterizer in the same (discretized) semantics, the torch restatement of
+  the splat and its autograd. Images: elementwise against 1e-5 relative /
+  1e-6 absolute (`image_tol_ratio` <= 1 passes). Gradients of each mesh:
+  max abs difference over the largest magnitude (`max_rel_err_grad`, bar
+  1e-4). Vertex gradients are compared per image only where every image has
+  its own mesh."""
+  n = min(16, len(wl.meshes), len(gpu["images"]))
+  t0 = time.perf_counter()
+  res = {}
+  for i in range(n):
+    res.update(cpu_port_sample(wl, 0.0, threads, images=[i], kind="oracle", keep=True)[3])
+    if time.perf_counter() - t0 >= budget_s:
+      break
+  per_mesh = len({id(m) for m in wl.meshes}) == len(wl.meshes)
+  img_ratio = img_abs = img_rel = grad_rel = 0.0
+  for i, (out, gv, gc) in res.items():
+    a, b = gpu["images"][i], out
+    d = np.abs(a - b)
+    img_abs = max(img_abs, float(d.max()))
+    img_ratio = max(img_ratio, float((d / (1e-6 + 1e-5 * np.abs(b))).max()))
+    big = np.abs(b) >= 1e-3
+    if big.any():
+      img_rel = max(img_rel, float((d[big] / np.abs(b[big])).max()))
+    if per_mesh:
+      for g_gpu, g_cpu in ((gpu["g_v"][i], gv), (gpu["g_c"][i], gc)):
+        if g_cpu is None:
+          continue
+        scale = float(np.abs(g_cpu).max()) or 1.0
+        grad_rel = max(grad_rel, float(np.abs(g_gpu - g_cpu).max()) / scale)
+  return {"images_checked": len(res), "max_abs_err_image": img_abs,
+          "max_rel_err_image": img_rel, "image_tol_ratio": img_ratio,
+          "max_rel_err_grad": grad_rel if per_mesh else None,
+          "within_tolerance": bool(img_ratio <= 1.0 and (not per_mesh or grad_rel <= 1e-4)),
+          "cpu_side": "C restatement of the reference CUDA rasterizer (bit-exact) + torch "
+                      "float32 restatement of the JAX splat with autograd"}
+
+
+def bench_config(wl):
+  """The `config` both arms print: the workload and its sizes."""
+  return {"workload": wl.desc, "num_images": len(wl.meshes), "total_mpix": wl.pixels / 1e6,
+          "total_triangles": wl.triangles, "num_layers": wl.num_layers,
+          "l2": "per-step working set of several GB > 129 MB L2"}
 
 
 def run_reference(args):
-  """The reference arm: the CPU port of the reference's path (see
-  cpu_port_sample) on the machine's host cores. Step i renders image i mod N of
-  the workload forward and backward; the value is the timed steps' pixels
-  over their time."""
+  """The reference arm, on the machine's host cores: the reference's own C++
+  CPU rasterizer for the raster stage (built from the reference sources by
+  oracle/Makefile) and the torch CPU restatement of the reference's JAX
+  splat and its autodiff (JAX is not installed). Step i renders image
+  i mod N of the workload forward and backward; the value is the timed
+  steps' pixels over their time."""
+  from oracle import raster
   wl = Workload(args.workload, args.num_meshes)
+  if raster.build_reference() is None:
+    print(json.dumps({"impl": "reference", "unavailable": "the reference CPU rasterizer's "
+                      "sources are not present (oracle/_ref/src or DIFFREN_REFERENCE)"}))
+    return
   threads = os.cpu_count() or 1
   n = len(wl.meshes)
   px_t = secs_t = 0.0
   for it in range(args.warmup + args.steps):
-    px, secs, _ = cpu_port_sample(wl, 0.0, threads, images=[it % n])
+    px, secs, _, _ = cpu_port_sample(wl, 0.0, threads, images=[it % n], kind="reference")
     if it >= args.warmup:
       px_t += px
       secs_t += secs
   value = px_t / secs_t / 1e6
-  sample = ("one image per step (images %d..%d of %d, cycling), %d px in %.1f s"
-            % (args.warmup % n, (args.warmup + args.steps - 1) % n, n, px_t, secs_t))
+  sample = ("one image of the workload per step (images %d..%d of %d, cycling), %d px in "
+            "%.1f s; rasterizer: the reference's own C++ CPU rasterizer, one thread per "
+            "image; splat fwd+bwd: torch float32 restatement of the JAX path on %d threads"
+            % (args.warmup % n, (args.warmup + args.steps - 1) % n, n, px_t, secs_t, threads))
   line = {
       "metric": "RtS fwd+bwd Mpix/s on 1 GB300, batched vs plain, at 1e-5 rel err",
       "value": value, "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps,
       "warmup": args.warmup, "ms_per_step": secs_t * 1e3 / args.steps,
       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
       "data": "synthetic (seeded meshes, cameras and targets)", "impl": "reference",
-      "config": {"workload": wl.desc, "num_images": n, "total_mpix": wl.pixels / 1e6,
-                 "total_triangles": wl.triangles, "num_layers": wl.num_layers},
-      "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "port",
+      "config": bench_config(wl),
+      "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "reference",
                        "sample": sample},
       "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
               "d2h_bytes_per_step": 0},
@@ -660,13 +752,22 @@ def main():
   res = run_ours(args, rank, world, device)
   wl = res["wl"]
   cpu = None
+  parity = None
   if rank == 0 and not args.no_cpu_baseline:
+    from oracle import raster
     threads = os.cpu_count() or 1
-    px, secs, used = cpu_port_sample(wl, args.cpu_budget, threads)
-    cpu = {"value": px / secs / 1e6, "unit": "Mpix/s", "cores": threads, "kind": "port",
+    kind = "reference" if raster.build_reference() is not None else "port"
+    px, secs, used, _ = cpu_port_sample(wl, args.cpu_budget, threads,
+                                        kind="reference" if kind == "reference" else "oracle")
+    cpu = {"value": px / secs / 1e6, "unit": "Mpix/s", "cores": threads, "kind": kind,
            "sample": "first %d of %d images of the workload (%d px), fwd+bwd, %.1f s; "
-                     "rasterizer one image per thread, splat on all threads"
-                     % (used, len(wl.meshes), px, secs)}
+                     "rasterizer: %s, one image per thread; splat fwd+bwd: torch float32 "
+                     "restatement of the JAX path (JAX is not installed) on all threads"
+                     % (used, len(wl.meshes), px, secs,
+                        "the reference's own C++ CPU rasterizer" if kind == "reference"
+                        else "the C restatement")}
+  if rank == 0 and res["gpu"] is not None:
+    parity = parity_check(wl, res["gpu"], args.cpu_budget, os.cpu_count() or 1)
   if rank != 0:
     if world > 1:
       dist.destroy_process_group()
@@ -683,18 +784,17 @@ def main():
       "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
       "scaling": "weak", "vs_baseline": None, "dtype": "f32",
       "data": "synthetic (seeded meshes, cameras and targets)",
-      "config": {"workload": wl.desc, "num_images": len(wl.meshes),
-                 "total_mpix": wl.pixels / 1e6, "total_triangles": wl.triangles,
-                 "num_layers": wl.num_layers,
-                 "foreground_samples": res["fg"], "pixels_near_foreground": res["near"],
-                 "parallelism": "replicas" if world > 1 else "1 GPU",
-                 "l2": "per-step working set of several GB > 129 MB L2",
-                 "cuda_graph": True, "raster_tile_autotuned": res["tile"]},
+      "config": bench_config(wl),
+      "details": {"foreground_samples": res["fg"], "pixels_near_foreground": res["near"],
+                  "parallelism": "replicas" if world > 1 else "1 GPU",
+                  "cuda_graph": True, "raster_tile_autotuned": res["tile"],
+                  "depth_semantics": "discretized (the reference CUDA rasterizer's)"},
+      "parity": parity,
       "e2e": {"value": whole_job_mpix(world, wl.pixels, res["ms_e2e"]), "unit": "Mpix/s",
               "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
       "plain": None if res["plain"] is None else {
           "value": res["plain"]["value"], "unit": "Mpix/s",
-          "ms_per_step": res["plain"]["ms_per_step"],
+          "ms_per_step": res["plain"]["ms_per_step"], "steps": res["plain"]["steps"],
           "batched_over_plain": value / world / res["plain"]["value"]},
       "gpu_launches": res["launches"] * args.steps,
       "kernels_ms": {k: round(v, 4) for k, v in pk.items()},
