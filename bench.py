@@ -4,10 +4,11 @@ Workload (default `c5`): a ragged batch of 64 seeded meshes (noisy
 icospheres or triangle soups, 50/50), triangle counts lognormal (median 20k,
 sigma 1.2) clipped to [500, 500k], one camera per mesh on a sphere of radius
 3, square resolutions drawn from {256, 512, 1024}, 3 depth layers, back-face
-culling, RGB vertex colors with alpha 1 interpolated as an RGBA attribute and
-passed through by the deferred shader. One step = forward
+culling, RGBA vertex colors (RGB seeded, alpha 1) interpolated as an
+attribute and passed through by the deferred shader. One step = forward
 render of every image + L2 loss against fixed target images + backward to
-vertex positions and vertex colors.
+vertex positions and vertex colors (the optimized color parameter is the
+RGBA vertex color; the RGB gradients are its first three columns).
 
 Reported (one JSON line on rank 0):
   value      batched path: all images in one launch per kernel, the step
@@ -75,7 +76,7 @@ class Workload:
       meshes, cams, sizes = wl.ragged_batch(num_meshes, seed=seed)
       desc = ("ragged batch of %d meshes (icosphere|soup), T lognormal median 20k "
               "in [500, 500k], square res in {256,512,1024}, L=3, fwd+bwd L2 loss "
-              "wrt vertices and RGB" % num_meshes)
+              "wrt vertices and RGBA vertex colors" % num_meshes)
     elif name == "c2":
       m = wl.soup_workload(200000, seed=seed)
       eyes = wl.sphere_eyes(8, seed=seed + 1)
@@ -341,7 +342,9 @@ def run_ours(args, rank, world, device):
     cols_h = torch.from_numpy(wl.texture).pin_memory()
     uv = torch.from_numpy(np.concatenate([m.uvs for m in wl.meshes])).to(device)
   else:
-    cols_h = torch.from_numpy(np.concatenate([m.colors for m in wl.meshes])).pin_memory()
+    rgb = np.concatenate([m.colors for m in wl.meshes])
+    cols_h = torch.from_numpy(rgb if wl.lit else np.concatenate(
+        [rgb, np.ones_like(rgb[:, :1])], 1)).pin_memory()
   cams_h = torch.from_numpy(np.stack(wl.cams)).pin_memory()
   target = torch.from_numpy(np.concatenate([t.reshape(-1, 4) for t in wl.targets])).to(device)
   # Two sets of device inputs and outputs: the end-to-end loop below runs
@@ -360,7 +363,7 @@ def run_ours(args, rank, world, device):
       out = r.render(v, {"rgb": c, "normals": r.vertex_normals(v), "pos": v}, cams,
                      lit_shader)
     else:
-      out = r.render(v, {"rgba": rgba(c)}, cams, shader)
+      out = r.render(v, {"rgba": c}, cams, shader)
     loss, (gv, gc) = l2_loss_grads(out, target, (v, c))
     return dict(g_v=gv, g_c=gc.contiguous(), loss=loss, out=out.detach())
 
@@ -383,7 +386,7 @@ def run_ours(args, rank, world, device):
     vo = np.cumsum([0] + [len(m.vertices) for m in wl.meshes])
     gpu = {"images": [x.cpu().numpy() for x in r.images(res0["out"])[:nck]],
            "g_v": [res0["g_v"][vo[i]:vo[i + 1]].cpu().numpy() for i in range(nck)],
-           "g_c": [None if textured else res0["g_c"][vo[i]:vo[i + 1]].cpu().numpy()
+           "g_c": [None if textured else res0["g_c"][vo[i]:vo[i + 1], :3].cpu().numpy()
                    for i in range(nck)]}
   del res0
   # Foreground layer samples of the workload, and pixels within one pixel
@@ -509,7 +512,9 @@ def run_plain(wl, device, args):
   data = []
   for m, cam, (w, h), t in zip(wl.meshes, wl.cams, wl.sizes, wl.targets):
     data.append((torch.tensor(m.vertices, device=device),
-                 tex if textured else torch.tensor(m.colors, device=device),
+                 tex if textured else torch.tensor(
+                     m.colors if wl.lit else np.concatenate(
+                         [m.colors, np.ones_like(m.colors[:, :1])], 1), device=device),
                  torch.tensor(m.uvs, device=device) if textured else None,
                  torch.tensor(m.triangles, device=device),
                  torch.tensor(cam, device=device), w, h,
@@ -528,7 +533,7 @@ def run_plain(wl, device, args):
         out = render.render_triangles(v, attrs, tri, cam, w, h, lit_shader,
                                       num_layers=wl.num_layers)
       else:
-        out = render.render_triangles(v, {"rgba": rgba(c)}, tri, cam, w, h, shader,
+        out = render.render_triangles(v, {"rgba": c}, tri, cam, w, h, shader,
                                       num_layers=wl.num_layers)
       l2_loss_grads(out, tgt, (v, c))
 

@@ -15,6 +15,7 @@ DR_CULL_NONE, DR_CULL_BACK, DR_CULL_FRONT = 0, 1, 2
 DR_DEPTH_DISCRETIZED, DR_DEPTH_FLOAT = 0, 1
 DR_FLAG_INDEX_OUT_OF_RANGE = 1
 DR_FLAG_NONFINITE_VERTEX = 2
+DR_RASTER_FOREGROUND_ONLY = 1
 DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
@@ -45,7 +46,8 @@ class RasterConfig(ctypes.Structure):
   _fields_ = [("num_layers", ctypes.c_int32),
               ("face_culling_mode", ctypes.c_int32),
               ("depth_mode", ctypes.c_int32), ("tile_width", ctypes.c_int32),
-              ("tile_height", ctypes.c_int32), ("large_tiles", ctypes.c_int32)]
+              ("tile_height", ctypes.c_int32), ("large_tiles", ctypes.c_int32),
+              ("flags", ctypes.c_uint32)]
 
 
 SIGNATURES = {

@@ -32,10 +32,13 @@ class BatchRenderer:
                resolutions: Sequence, num_layers: int = 1,
                face_culling_mode=constants.FaceCullingMode.BACK,
                depth_semantics=constants.DepthSemantics.CUDA, device=None,
-               tile=(0, 0), large_tiles=0):
+               tile=(0, 0), large_tiles=0, recompute_raster=False):
     """``tile`` = (width, height) of the rasterizer's tiles, (0, 0) for the
     default, or "auto" to let the autotuner pick the tile and the
-    large-triangle threshold on the first render (see autotune.py)."""
+    large-triangle threshold on the first render (see autotune.py).
+    ``recompute_raster``: for memory-tight batches, the backward reruns the
+    rasterizer instead of keeping the triangle ids, barycentrics and vertex
+    ids of every layer sample from the forward (28 bytes per sample)."""
     if len(triangles) != len(vertex_counts) or len(triangles) != len(resolutions):
       raise ValueError("triangles, vertex_counts and resolutions differ in length")
     self.device = torch.device(device or "cuda")
@@ -55,6 +58,7 @@ class BatchRenderer:
                                         (0, 0) if self._autotune else tile, large_tiles)
     self.workspace = kernels.Workspace(self.device)
     self.workspace.get(kernels.raster_workspace_bytes(self.batch, self.config))
+    self.recompute_raster = bool(recompute_raster)
 
   def autotune(self, clip, attributes=None, **kw):
     """Picks the fastest tile / large-triangle configuration for this batch
@@ -123,8 +127,11 @@ class BatchRenderer:
     if fused:
       # One pass: the rasterizer's epilogue interpolates the attributes and
       # the splat positions of every layer sample.
+      # The splat path tells background samples by the depth buffer, so
+      # their ids and barycentrics need not be written.
       interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
-          cat, clip, self.triangles, b, self.config, self.workspace)
+          cat, clip, self.triangles, b, kernels.foreground_only(self.config), self.workspace,
+          self.recompute_raster)
     else:
       ids, z, bary = self.rasterize(clip)
       if splatting:

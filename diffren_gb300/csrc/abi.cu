@@ -38,6 +38,7 @@ dr_raster_config default_config(int32_t L, int32_t cull, int32_t depth_mode) {
   c.tile_width = 0;
   c.tile_height = 0;
   c.large_tiles = 0;
+  c.flags = 0;
   return c;
 }
 
@@ -51,7 +52,7 @@ extern "C" {
 
 const char* dr_last_error(void) { return g_error.c_str(); }
 
-int32_t dr_abi_version(void) { return 1; }
+int32_t dr_abi_version(void) { return 2; }
 
 size_t dr_rasterize_batch_workspace_bytes(const dr_image_desc* images,
                                           int32_t num_images,

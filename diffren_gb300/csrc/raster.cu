@@ -51,6 +51,7 @@ struct RasterArgs {
   const float4* verts;
   const int32_t* tris;
   int culling, depth_mode, L, TW, TH, large_tiles;
+  bool fg_only;  // DR_RASTER_FOREGROUND_ONLY: background ids / barycentrics unwritten
   int64_t total_tris;
   int32_t total_tiles;
   TriSetup* setup;
@@ -555,12 +556,14 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
           } else if (valid) {
             const int64_t o = base + l * HW + pix;
             const float b0[3] = {0.0f, 0.0f, 0.0f};
-            a.ids[o] = disc ? 0 : -1;
             a.z[o] = 1.0f;
-            float* bo = a.bary + 3 * o;
-            bo[0] = 0.0f;
-            bo[1] = 0.0f;
-            bo[2] = 0.0f;
+            if (!a.fg_only) {
+              a.ids[o] = disc ? 0 : -1;
+              float* bo = a.bary + 3 * o;
+              bo[0] = 0.0f;
+              bo[1] = 0.0f;
+              bo[2] = 0.0f;
+            }
             if (kFused) write_sample(a, B, img, nullptr, 1.0f, b0, o);
           }
         }
@@ -639,12 +642,14 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
             }
             if (!disc || zz != 1.0f) { b[0] = bb[0]; b[1] = bb[1]; b[2] = bb[2]; }
           }
-          a.ids[o] = id;
           a.z[o] = zz;
-          float* bo = a.bary + 3 * o;
-          bo[0] = b[0];
-          bo[1] = b[1];
-          bo[2] = b[2];
+          if (!a.fg_only || key != kEmpty) {
+            a.ids[o] = id;
+            float* bo = a.bary + 3 * o;
+            bo[0] = b[0];
+            bo[1] = b[1];
+            bo[2] = b[2];
+          }
           if (kFused) write_sample(a, B, img, st, zz, b, o);
         }
       }
@@ -733,6 +738,10 @@ bool check_config(const dr_raster_config* cfg, int& L, int& TW, int& TH, int& la
   }
   if (TW > 128 || TH > 128 || TW * TH > 1024) {
     err = "tile must satisfy width, height <= 128 and width*height <= 1024";
+    return false;
+  }
+  if ((cfg->flags & ~DR_RASTER_FOREGROUND_ONLY) != 0) {
+    err = "unknown raster config flags";
     return false;
   }
   return true;
@@ -831,6 +840,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     a.tris = triangles;
     a.culling = cfg->face_culling_mode;
     a.depth_mode = cfg->depth_mode;
+    a.fg_only = (cfg->flags & DR_RASTER_FOREGROUND_ONLY) != 0;
     a.L = L; a.TW = TW; a.TH = TH; a.large_tiles = large;
     a.total_tris = tris;
     a.total_tiles = tiles;

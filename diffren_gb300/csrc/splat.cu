@@ -418,7 +418,8 @@ struct SplatArgs {
   int64_t P;     // pixels covered by the call: plane stride of `saved`
   float coef;
   float* out;
-  float* saved;  // [3 (C+1), P] planar accumulators (forward out, backward in)
+  float* saved;  // [3 (C+1) + 1, P] planar accumulators and surface codes
+                 // (forward out, backward in)
   float* accum;
   float* normalized;
   const float* d_out;
@@ -716,6 +717,7 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
 
   float acc[3][4 * Q];
   float wacc[3] = {0.0f, 0.0f, 0.0f};
+  unsigned code = 0;  // surface codes of the 9 taps (three layers only)
   if (layers == 0) {
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -735,6 +737,9 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
       const int s = p - v * kRS - u;
       const unsigned m = in ? (wide ? unsigned(fgm16[s]) : unsigned(fgm8[s])) : 0u;
       tap[j] = m ? m | (unsigned(surface_index(zs, s, p, L) + 16) << 16) : 0u;
+      // Surface index + 2 in 3 bits per tap (three layers: -2..2) for the
+      // VJP, which then needs no depths.
+      if (LT == 3 && tap[j]) code |= ((tap[j] >> 16) - 14u) << (3 * j);
     }
     // Class 0 = in front of the surface, 1 = at it, 2 = behind it
     // (splat.py:149-162), accumulated layer by layer.
@@ -799,6 +804,7 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
       for (int c = 0; c < C; ++c) a.saved[(k * (C + 1) + c) * a.P + pix] = acc[k][c];
       a.saved[(k * (C + 1) + C) * a.P + pix] = wacc[k];
     }
+    if (LT == 3) reinterpret_cast<unsigned*>(a.saved)[3 * (C + 1) * a.P + pix] = code;
   }
   if (a.accum || a.normalized) {
     const int64_t HW = int64_t(W) * H;
@@ -954,7 +960,12 @@ __global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
       load_row<C>(a.d_out + pix * C, d);
       accum_adjoint<C>(acc, wacc, d, g, h);
       const int64_t eq = lbase + int64_t(qy) * W + qx;
-      if (a.zb) {
+      if (LT == 3 && a.zb) {
+        // The forward's surface codes of this pixel's taps replace the
+        // depths (the zs area holds them).
+        reinterpret_cast<unsigned*>(zs)[i] =
+            __ldg(reinterpret_cast<const unsigned*>(a.saved) + 3 * (C + 1) * a.P + pix);
+      } else if (a.zb) {
         unsigned m = 0;
         for (int l = 0; l < L; ++l) m |= unsigned(__ldg(a.zb + eq + l * HW) != 1.0f) << l;
         for (int l = 0; l < L; ++l)
@@ -999,7 +1010,12 @@ __global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
       const int px = sx + u, py = sy + v;
       const bool in = mine && px >= 0 && py >= 0 && px < W && py < H;
       ok |= unsigned(in) << j;
-      surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
+      if (LT == 3)  // pixel s1 + (u, v) saw this sample as its tap j
+        surf[j] = in ? int((reinterpret_cast<const unsigned*>(zs)[s1 + v * kRS + u] >>
+                            (3 * j)) & 7u) - 2
+                     : 0;
+      else
+        surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
     }
     constexpr int kL = LT > 0 ? LT : 1;
     unsigned masks[kL];

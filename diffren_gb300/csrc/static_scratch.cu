@@ -131,6 +131,7 @@ extern "C" int dr_rasterize_triangles_static_scratch(
   c.tile_width = 0;
   c.tile_height = 0;
   c.large_tiles = 0;
+  c.flags = 0;
   // Size check first: nothing runs on the GPU for an oversized request.
   const size_t need = dr::raster_workspace_bytes(&d, 1, &c, err);
   int rc = DR_OK;

@@ -163,14 +163,22 @@ class ImageBatch:
 
 
 def raster_config(num_layers, face_culling_mode, depth_mode, tile=(0, 0),
-                  large_tiles=0):
+                  large_tiles=0, flags=0):
   c = RasterConfig()
   c.num_layers = int(num_layers)
   c.face_culling_mode = int(face_culling_mode)
   c.depth_mode = int(depth_mode)
   c.tile_width, c.tile_height = int(tile[0]), int(tile[1])
   c.large_tiles = int(large_tiles)
+  c.flags = int(flags)
   return c
+
+
+def foreground_only(config):
+  """A copy of `config` with DR_RASTER_FOREGROUND_ONLY set."""
+  return raster_config(config.num_layers, config.face_culling_mode, config.depth_mode,
+                       (config.tile_width, config.tile_height), config.large_tiles,
+                       config.flags | _lib.DR_RASTER_FOREGROUND_ONLY)
 
 
 class Workspace:
@@ -569,10 +577,16 @@ def _viewport_tangent(q, dc, z, batch, L, w_from_vp):
 class _RasterSamples(torch.autograd.Function):
   """Rasterization fused with attribute interpolation and splat positions;
   the VJP is that of the fused pass (the rasterizer's own outputs carry no
-  gradient, as in the reference)."""
+  gradient, as in the reference).
+
+  With ``recompute`` the forward keeps for the VJP only what the splat
+  keeps anyway (depth and positions) plus the inputs: the triangle ids,
+  barycentrics and vertex ids (28 bytes per layer sample) are not stored
+  but recomputed in the backward by running the rasterizer again, which
+  gives the same bits. This trades one rasterizer pass for memory."""
 
   @staticmethod
-  def forward(ctx, attributes, clip, triangles, batch, config, workspace):
+  def forward(ctx, attributes, clip, triangles, batch, config, workspace, recompute=False):
     lib = _lib.load()
     dev = clip.device
     L = config.num_layers
@@ -583,7 +597,7 @@ class _RasterSamples(torch.autograd.Function):
     bary = torch.empty(n, 3, dtype=torch.float32, device=dev)
     out = torch.empty(n, K, dtype=torch.float32, device=dev)
     vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
-    vids = torch.empty(n, 3, dtype=torch.int32, device=dev)
+    vids = None if recompute else torch.empty(n, 3, dtype=torch.int32, device=dev)
     ws = workspace.get(raster_workspace_bytes(batch, config))
     with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
       rc = lib.dr_rasterize_batch_interpolate(
@@ -591,7 +605,12 @@ class _RasterSamples(torch.autograd.Function):
           _p(bary), _p(attributes), K, _p(out), _p(vp), _p(vids), _p(ws), ws.numel(),
           _stream(dev))
     _lib.check(rc, "dr_rasterize_batch_interpolate")
-    ctx.save_for_backward(attributes, clip, bary, triangles, ids, z, vp, vids)
+    ctx.recompute = bool(recompute)
+    if recompute:
+      ctx.save_for_backward(attributes, clip, triangles, z, vp)
+      ctx.config, ctx.workspace = config, workspace
+    else:
+      ctx.save_for_backward(attributes, clip, bary, triangles, ids, z, vp, vids)
     ctx.save_for_forward(bary, triangles, ids, z, vp)
     ctx.batch, ctx.L, ctx.num_channels = batch, L, K
     ctx.set_materialize_grads(False)
@@ -620,26 +639,54 @@ class _RasterSamples(torch.autograd.Function):
 
   @staticmethod
   def backward(ctx, d_out, d_vp, *unused):
-    attributes, clip, bary, triangles, ids, z, vp, vids = ctx.saved_tensors
+    if ctx.recompute:
+      attributes, clip, triangles, z, vp = ctx.saved_tensors
+      ids, bary, vids = _rerasterize(ctx, clip, triangles)
+    else:
+      attributes, clip, bary, triangles, ids, z, vp, vids = ctx.saved_tensors
     d_attr, d_clip, _ = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles,
                                      ids, z, False, vp, vids)
     return (d_attr if ctx.needs_input_grad[0] else None,
-            d_clip if ctx.needs_input_grad[1] else None, None, None, None, None)
+            d_clip if ctx.needs_input_grad[1] else None, None, None, None, None, None)
 
 
-def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, workspace):
+def _rerasterize(ctx, clip, triangles):
+  """The forward's triangle ids, barycentrics and vertex ids, recomputed
+  (the rasterizer is deterministic: same inputs, same bits)."""
+  lib = _lib.load()
+  dev = clip.device
+  n = ctx.L * ctx.batch.total_pixels
+  ids = torch.empty(n, dtype=torch.int32, device=dev)
+  z = torch.empty(n, dtype=torch.float32, device=dev)
+  bary = torch.empty(n, 3, dtype=torch.float32, device=dev)
+  vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
+  vids = torch.empty(n, 3, dtype=torch.int32, device=dev)
+  ws = ctx.workspace.get(raster_workspace_bytes(ctx.batch, ctx.config))
+  with torch.cuda.device(dev), _op("raster_recompute", 4 * _groups(ctx.batch)):
+    rc = lib.dr_rasterize_batch_interpolate(
+        _p(clip), _p(triangles), ctx.batch.ptr, ctx.batch.n, ctypes.byref(ctx.config),
+        _p(ids), _p(z), _p(bary), None, 0, None, _p(vp), _p(vids), _p(ws), ws.numel(),
+        _stream(dev))
+  _lib.check(rc, "dr_rasterize_batch_interpolate")
+  return ids, bary, vids
+
+
+def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, workspace,
+                                 recompute=False):
   """Rasterizes a packed batch and, in the same pass, interpolates
   ``attributes`` [sum V, K <= 16] (background 0) and computes the splat
   positions. Returns (attributes [L*P, K], positions [L*P, 4], ids, z, bary);
   the first two are differentiable w.r.t. ``attributes`` and ``clip``.
   Positions are written for foreground samples only, as (viewport xyz,
   clip w): splat them with ``z`` so that the depth buffer marks the
-  background."""
+  background. With ``recompute`` the VJP reruns the rasterizer instead of
+  keeping ids, barycentrics and vertex ids from the forward."""
   _require_cuda(clip, triangles)
   attributes = _f32(attributes)
   if attributes.shape[1] > _lib.DR_MAX_CHANNELS:
     raise ValueError("at most %d attribute channels" % _lib.DR_MAX_CHANNELS)
-  return _RasterSamples.apply(attributes, clip, triangles, batch, config, workspace)
+  return _RasterSamples.apply(attributes, clip, triangles, batch, config, workspace,
+                              bool(recompute))
 
 
 def interpolate_with_positions_packed(attributes, clip, bary, triangles, ids, z, batch,
@@ -718,7 +765,7 @@ class _Splat(torch.autograd.Function):
     P = batch.total_pixels
     out = torch.empty(P, C, dtype=torch.float32, device=dev)
     needs_grad = positions.requires_grad or colors.requires_grad
-    saved = (torch.empty(3 * (C + 1), P, dtype=torch.float32, device=dev)
+    saved = (torch.empty(3 * (C + 1) + 1, P, dtype=torch.float32, device=dev)
              if needs_grad else None)
     accum = norm = None
     if want_accum:

@@ -38,7 +38,7 @@ def _shade_layers(shading_function, interpolated, num_layers, batched):
 
 
 def _render_fused(geom, attributes, shading_function, num_layers, face_culling_mode,
-                  depth_semantics, return_accum_buffers):
+                  depth_semantics, return_accum_buffers, recompute_raster=False):
   """SPLAT_OVER through the rasterizer that interpolates the attributes and
   the splat positions in its epilogue; None when the attributes exceed its
   channel limit."""
@@ -54,10 +54,13 @@ def _render_fused(geom, attributes, shading_function, num_layers, face_culling_m
   if sum(widths) > kernels._lib.DR_MAX_CHANNELS:
     return None
   cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0].contiguous()
-  cfg = kernels.raster_config(num_layers, face_culling_mode, int(depth_semantics))
+  # Background samples are told by the depth buffer downstream, so their
+  # ids and barycentrics need not be written.
+  cfg = kernels.raster_config(num_layers, face_culling_mode, int(depth_semantics),
+                              flags=kernels._lib.DR_RASTER_FOREGROUND_ONLY)
   interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
       cat, geom.clip, geom.triangles_packed, geom.batch, cfg,
-      kernels.default_workspace(geom.clip.device))
+      kernels.default_workspace(geom.clip.device), recompute_raster)
   frame = rasterize.framebuffer_of(geom, num_layers, ids, z, bary)
   lead = (geom.B,) if geom.batched else ()
   interp = interp.view(*lead, num_layers, frame.height, frame.width, -1)
@@ -74,11 +77,15 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
                      face_culling_mode=constants.FaceCullingMode.BACK,
                      compositing_mode=constants.CompositingMode.SPLAT_OVER,
                      return_accum_buffers=False, compute_diff_barys=False,
-                     depth_semantics=constants.DepthSemantics.CUDA):
+                     depth_semantics=constants.DepthSemantics.CUDA,
+                     recompute_raster=False):
   """Rendering with differentiable occlusion using rasterize-then-splat.
 
   Returns [H, W, C] ([num_layers, H, W, C] for CompositingMode.NONE), with a
-  leading batch dimension when the inputs are batched.
+  leading batch dimension when the inputs are batched. ``recompute_raster``
+  (SPLAT_OVER, beyond the reference's arguments): the backward reruns the
+  rasterizer instead of keeping its per-sample triangle ids, barycentrics
+  and vertex ids, for memory-tight renders.
 
   Raises:
     ValueError: if face_culling_mode is not BACK and compositing_mode is
@@ -96,7 +103,8 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   if (compositing_mode == constants.CompositingMode.SPLAT_OVER and not compute_diff_barys
       and attributes):
     fused = _render_fused(geom, attributes, shading_function, num_layers,
-                          face_culling_mode, depth_semantics, return_accum_buffers)
+                          face_culling_mode, depth_semantics, return_accum_buffers,
+                          recompute_raster)
     if fused is not None:
       return fused
   frame, _ = rasterize.rasterize_geometry(geom, num_layers, face_culling_mode,

@@ -103,7 +103,15 @@ typedef struct dr_raster_config {
   int32_t tile_height;       /* 0 = default (16); tile_width*tile_height <= 1024 */
   int32_t large_tiles;       /* triangles spanning more tiles than this go to a
                                 per-image list every tile scans; 0 = default */
+  uint32_t flags;            /* DR_RASTER_* bits, 0 = none */
 } dr_raster_config;
+
+/* dr_raster_config.flags: background samples (z = 1) get their depth (and,
+ * in dr_rasterize_batch_interpolate, zero attributes) but their triangle id
+ * and barycentrics are left unwritten. For callers that tell background
+ * samples by the depth buffer, as the splat path does; saves 16 bytes per
+ * background layer sample. */
+#define DR_RASTER_FOREGROUND_ONLY 1u
 
 #define DR_MAX_LAYERS 16
 #define DR_MAX_CHANNELS 16
@@ -386,10 +394,12 @@ int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
  * them unwritten; without it every position is read and its w is the
  * foreground flag. colors [L, H, W, C]
  * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
- * saved [3, C + 1, P] receives the fg/surface/bg accumulators and weights
- * the VJP needs, one plane of P pixels per value, P = the largest
- * pixel_offset + width * height of the images (nullable; written only near
- * foreground samples, where dr_splat_bwd reads it); accum and normalized [3, H, W, C] are
+ * saved [3 (C + 1) + 1, P] receives the fg/surface/bg accumulators and
+ * weights the VJP needs, one plane of P pixels per value, P = the largest
+ * pixel_offset + width * height of the images, and in its last plane (for
+ * three layers) each pixel's surface classes of its 9 taps as 32-bit codes
+ * (nullable; written only near foreground samples, where dr_splat_bwd reads
+ * it); accum and normalized [3, H, W, C] are
  * the reference's debugging buffers (nullable). With C % 4 == 0 the color
  * and output buffers must be 16-byte aligned. */
 int dr_splat_fwd(const float* positions, const float* z_buffer, const float* colors,

@@ -45,7 +45,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_error_string():
   lib = _lib.load()
-  assert lib.dr_abi_version() == 1
+  assert lib.dr_abi_version() == 2
   assert isinstance(lib.dr_last_error(), bytes)
 
 

@@ -230,3 +230,72 @@ def test_batch_renderer_over_and_none_match_per_image(mode, device):
     sl = slice(int(coff[i]), int(coff[i + 1]))
     scale = float(gci.abs().max()) or 1.0
     torch.testing.assert_close(gc[sl], gci, rtol=1e-4, atol=1e-5 * scale)
+
+
+@pytest.mark.parametrize("use_batch", [True, False])
+def test_recompute_raster_gives_the_same_gradients(use_batch, device):
+  """recompute_raster reruns the rasterizer in the backward instead of
+  keeping its per-sample ids, barycentrics and vertex ids: same image and
+  same gradients (the vertex-gradient atomics may reorder float sums, so
+  within 1e-6 of the largest magnitude), and fewer bytes kept for the VJP."""
+  meshes, cams, sizes = workloads.ragged_batch(5, seed=7, median_triangles=3000,
+                                               resolutions=(64, 96, 128))
+
+  def run(recompute):
+    torch.cuda.synchronize(device)
+    base = torch.cuda.memory_allocated(device)
+    if use_batch:
+      r = batch_lib.BatchRenderer([m.triangles for m in meshes],
+                                  [len(m.vertices) for m in meshes], sizes, num_layers=3,
+                                  device=device, recompute_raster=recompute)
+      v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device,
+                       requires_grad=True)
+      c = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device,
+                       requires_grad=True)
+      out = r.render(v, {"rgb": c}, torch.tensor(np.stack(cams), device=device),
+                     lambda a: torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1))
+    else:
+      m, cam, (w, h) = meshes[0], cams[0], sizes[0]
+      v = torch.tensor(m.vertices, device=device, requires_grad=True)
+      c = torch.tensor(m.colors, device=device, requires_grad=True)
+      out = render.render_triangles(
+          v, {"rgb": c}, torch.tensor(m.triangles, device=device), torch.tensor(cam, device=device),
+          w, h, lambda a: torch.cat([a["rgb"], torch.ones_like(a["rgb"][..., :1])], -1),
+          num_layers=3, recompute_raster=recompute)
+    kept = torch.cuda.memory_allocated(device) - base
+    gv, gc = torch.autograd.grad(out.square().sum(), (v, c))
+    return out.detach(), gv, gc, kept
+
+  o0, gv0, gc0, kept0 = run(False)
+  o1, gv1, gc1, kept1 = run(True)
+  assert torch.equal(o0, o1)
+  for a, b in ((gv0, gv1), (gc0, gc1)):
+    assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
+  assert kept1 < kept0
+
+
+def test_foreground_only_flag_writes_the_same_foreground(device):
+  """DR_RASTER_FOREGROUND_ONLY leaves background ids and barycentrics
+  unwritten; depth, foreground ids / barycentrics, attributes (background
+  0) and foreground positions are the same bits as without it."""
+  meshes, cams, sizes = workloads.ragged_batch(6, seed=11, median_triangles=4000,
+                                               resolutions=(64, 128, 160))
+  from oracle import raster
+  clips = [raster.transform(c, m.vertices) for m, c in zip(meshes, cams)]
+  batch = kernels.ImageBatch([s[0] for s in sizes], [s[1] for s in sizes],
+                             [len(c) for c in clips], [len(m.triangles) for m in meshes])
+  v = torch.as_tensor(np.concatenate(clips), device=device)
+  t = torch.as_tensor(np.concatenate([m.triangles for m in meshes]), device=device)
+  attrs = torch.rand(v.shape[0], 4, device=device)
+  outs = []
+  for cfg in (kernels.raster_config(3, 1, 0),
+              kernels.foreground_only(kernels.raster_config(3, 1, 0))):
+    with torch.no_grad():
+      outs.append(kernels.rasterize_interpolate_packed(attrs, v, t, batch, cfg,
+                                                       kernels.Workspace(device)))
+  (a0, p0, i0, z0, b0), (a1, p1, i1, z1, b1) = outs
+  fg = z0 != 1.0
+  assert torch.equal(z0, z1) and torch.equal(a0, a1)
+  assert torch.equal(i0[fg], i1[fg]) and torch.equal(b0[fg], b1[fg])
+  assert torch.equal(p0[fg], p1[fg])
+  assert (a1[~fg] == 0).all()
