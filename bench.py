@@ -286,13 +286,15 @@ def kernel_bytes(wl, fg, near=None, C=4, K=4):
       # every sample and the viewport position of every foreground sample out
       "raster": T * 12 + V * (16 + 4 * K) + S * (20 + 4 * K) + 16 * fg,
       # depth of every sample, position and color of every foreground
-      # sample in; composited color and saved accumulators (3 (C + 1)) per
-      # pixel out
-      "splat_fwd": 4 * S + (16 + 4 * C) * fg + 4 * C * P + 12 * (C + 1) * near,
-      # saved accumulators and d color per pixel, depth of every sample,
-      # position and color of the foreground ones in; d color of every
-      # sample and d position of every foreground sample out
-      "splat_bwd": near * (12 * (C + 1) + 4 * C) + 4 * S + (16 + 4 * C) * fg + 4 * C * S + 16 * fg,
+      # sample in; composited color per pixel, saved accumulators (3 (C + 1))
+      # and the surface code per pixel near foreground out
+      "splat_fwd": 4 * S + (16 + 4 * C) * fg + 4 * C * P + (12 * (C + 1) + 4) * near,
+      # saved accumulators, surface code and d color per pixel near
+      # foreground, depth of every sample, position and color of the
+      # foreground ones in; d color of every sample and d position of every
+      # foreground sample out
+      "splat_bwd": (near * (12 * (C + 1) + 4 + 4 * C) + 4 * S + (16 + 4 * C) * fg + 4 * C * S
+                    + 16 * fg),
       # z of every sample; ids, bary, d position and d attributes of the
       # depth of every sample; barycentrics, vertex indices, d position,
       # position and d attributes of the foreground ones; vertex gradients

@@ -418,8 +418,9 @@ struct SplatArgs {
   int64_t P;     // pixels covered by the call: plane stride of `saved`
   float coef;
   float* out;
-  float* saved;  // [3 (C+1) + 1, P] planar accumulators and surface codes
-                 // (forward out, backward in)
+  float* saved;  // [3 (C+1) + 2, P] planar accumulators, surface codes and
+                 // the tile list (forward out; the backward reads it and
+                 // resets its own work counter in it)
   float* accum;
   float* normalized;
   const float* d_out;
@@ -515,9 +516,8 @@ struct TileRef {
   int img, x0, y0;
 };
 
-__device__ __forceinline__ TileRef tile_of(const Batch& B) {
+__device__ __forceinline__ TileRef tile_at(const Batch& B, int item) {
   TileRef t;
-  const int item = blockIdx.x;
   t.img = find_segment(B.tile_start, B.n, item);
   const int local = item - B.tile_start[t.img];
   const int ntx = B.tiles_x[t.img];
@@ -525,6 +525,18 @@ __device__ __forceinline__ TileRef tile_of(const Batch& B) {
   t.y0 = (local / ntx) * kTY;
   return t;
 }
+
+__device__ __forceinline__ TileRef tile_of(const Batch& B) { return tile_at(B, blockIdx.x); }
+
+// The tiles of a splat call whose sample region (tile + 1-pixel halo) holds
+// a foreground sample, listed by splat_classify_kernel; the heavy splat
+// kernels then run only on those, and the empty tiles' outputs are zeros.
+struct TileList {
+  unsigned* count;      // [0] tiles listed, [1] / [2] work counters of the
+                        // forward / backward kernels over the list
+  int* list;            // listed tile items (in any order)
+  unsigned char* flag;  // per tile: 1 when listed
+};
 
 // Surface index of the splat from sample s reaching pixel p
 // (splat.py:131-145): c = argmin_k |zS_k - zD_0|, t = argmin_k |zD_k - zS_0|
@@ -577,11 +589,10 @@ __device__ __forceinline__ void accumulate(float2 (&acc)[2 * Q], float& wacc, co
 // LT > 0 fixes the layer count at compile time (the common L = 3 case), so
 // the layer loops unroll; LT = 0 reads it from the arguments.
 template <int C, int LT>
-__global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArgs a, Batch B) {
+__device__ __forceinline__ void splat_fwd_tile(const SplatArgs& a, const Batch& B, int item,
+                                               float* smem, unsigned& s_layers) {
   constexpr int Q = Groups<C>::Q;
-  extern __shared__ __align__(16) float smem[];
-  __shared__ unsigned s_layers;
-  const TileRef tr = tile_of(B);
+  const TileRef tr = tile_at(B, item);
   const int L = LT > 0 ? LT : a.L;
   float* zs = smem;
   float* wx = zs + L * kRR;
@@ -817,6 +828,67 @@ __global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArg
   }
 }
 
+// One block per tile.
+template <int C, int LT>
+__global__ void __launch_bounds__(256, C <= 4 ? 5 : 3) splat_fwd_kernel(SplatArgs a, Batch B) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ unsigned s_layers;
+  splat_fwd_tile<C, LT>(a, B, blockIdx.x, smem, s_layers);
+}
+
+// Persistent blocks over the listed tiles; a work counter hands them out.
+template <int C, int LT>
+__global__ void __launch_bounds__(256, C <= 4 ? 5 : 3)
+    splat_fwd_list_kernel(SplatArgs a, Batch B, TileList t) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ unsigned s_layers;
+  __shared__ int s_item;
+  const int n = int(t.count[0]);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = int(atomicAdd(t.count + 1, 1u));
+    __syncthreads();
+    const int w = s_item;
+    if (w >= n) break;
+    splat_fwd_tile<C, LT>(a, B, t.list[w], smem, s_layers);
+    __syncthreads();
+  }
+}
+
+// One warp per tile: lists the tiles whose region holds a foreground
+// sample (its layer 0 is foreground: layers fill front to back, so a
+// background layer 0 has only background behind it) and writes zeros to
+// the image of the others.
+template <int C>
+__global__ void __launch_bounds__(256) splat_classify_kernel(SplatArgs a, Batch B, TileList t,
+                                                             int tiles) {
+  const int item = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (item >= tiles) return;
+  const int lane = threadIdx.x & 31;
+  const TileRef tr = tile_at(B, item);
+  const int W = B.width[tr.img], H = B.height[tr.img];
+  const int64_t base = int64_t(a.L) * B.pix_off[tr.img];
+  bool fg = false;
+#pragma unroll 4
+  for (int i = lane; i < kRR; i += 32) {
+    const int ry = i / kRS;
+    const int x = tr.x0 - 1 + (i - ry * kRS), y = tr.y0 - 1 + ry;
+    if (x >= 0 && y >= 0 && x < W && y < H) fg |= __ldg(a.zb + base + int64_t(y) * W + x) != 1.0f;
+  }
+  fg = __any_sync(0xffffffffu, fg);
+  if (lane == 0) {
+    t.flag[item] = fg ? 1 : 0;
+    if (fg) t.list[atomicAdd(t.count, 1u)] = item;
+  }
+  if (fg) return;
+  float zero[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) zero[c] = 0.0f;
+  for (int p = lane; p < kTX * kTY; p += 32) {
+    const int px = tr.x0 + p % kTX, py = tr.y0 + p / kTX;
+    if (px < W && py < H) store_row<C>(a.out + (B.pix_off[tr.img] + int64_t(py) * W + px) * C, zero);
+  }
+}
+
 // Adjoints of the accumulators at one pixel, from d_out through the over
 // compositing and the normalization (jnp.maximum splits its gradient 0.5 /
 // 0.5 at equality, as lax.max does).
@@ -903,11 +975,10 @@ __device__ __forceinline__ void sample_adjoint(const Taps& tp, const float4* col
 // layers the register bound lets five blocks share an SM, the count the
 // shared memory allows (a few bytes of spills, measured faster than four).
 template <int C, int LT>
-__global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
-    splat_bwd_kernel(SplatArgs a, Batch B) {
+__device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& B, int item,
+                                               float* smem) {
   constexpr int Q = Groups<C>::Q;
-  extern __shared__ __align__(16) float smem[];
-  const TileRef tr = tile_of(B);
+  const TileRef tr = tile_at(B, item);
   const int L = LT > 0 ? LT : a.L;
   const int W = B.width[tr.img], H = B.height[tr.img];
   const int64_t HW = int64_t(W) * H;
@@ -1113,6 +1184,57 @@ __global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
   }
 }
 
+template <int C, int LT>
+__global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
+    splat_bwd_kernel(SplatArgs a, Batch B) {
+  extern __shared__ __align__(16) float smem[];
+  splat_bwd_tile<C, LT>(a, B, blockIdx.x, smem);
+}
+
+// Persistent blocks over the tiles the forward listed, handed out by the
+// backward's work counter (reset by splat_bwd_zero_kernel, which runs first).
+template <int C, int LT>
+__global__ void __launch_bounds__(256, (C <= 4 && LT == 3) ? 5 : 4)
+    splat_bwd_list_kernel(SplatArgs a, Batch B, TileList t) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_item;
+  const int n = int(t.count[0]);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = int(atomicAdd(t.count + 2, 1u));
+    __syncthreads();
+    const int w = s_item;
+    if (w >= n) break;
+    splat_bwd_tile<C, LT>(a, B, t.list[w], smem);
+    __syncthreads();
+  }
+}
+
+// One warp per tile that the forward did not list: no foreground sample in
+// the region, so every sample of the tile gets a zero color gradient (with
+// a depth buffer their position gradients stay unwritten). Also resets the
+// backward's work counter.
+template <int C>
+__global__ void __launch_bounds__(256) splat_bwd_zero_kernel(SplatArgs a, Batch B, TileList t,
+                                                             int tiles) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) t.count[2] = 0u;
+  const int item = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (item >= tiles || t.flag[item]) return;
+  const int lane = threadIdx.x & 31;
+  const TileRef tr = tile_at(B, item);
+  const int W = B.width[tr.img], H = B.height[tr.img];
+  const int64_t HW = int64_t(W) * H;
+  const int64_t lbase = int64_t(a.L) * B.pix_off[tr.img];
+  float zero[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) zero[c] = 0.0f;
+  for (int p = lane; p < kTX * kTY; p += 32) {
+    const int px = tr.x0 + p % kTX, py = tr.y0 + p / kTX;
+    if (px >= W || py >= H) continue;
+    const int64_t e = lbase + int64_t(py) * W + px;
+    for (int l = 0; l < a.L; ++l) store_row<C>(a.d_colors + (e + l * HW) * C, zero);
+  }
+}
+
 
 // Forward-mode derivative (JVP) of splat + normalize + over for tangents of
 // the sample positions (x, y) and, optionally, of the colors, with the
@@ -1267,28 +1389,96 @@ size_t bwd_smem(int L, int C) {
   return size_t(L + 3 * 4 * ((C + 3) / 4) + 3) * kRR * 4;
 }
 
+// The tile list lives in the last plane of the saved buffer (plane
+// 3 (C + 1) + 1): the counters, the list, then one flag byte per tile.
+constexpr size_t kListHeader = 16;
+size_t list_bytes(int tiles) {
+  return kListHeader + ((size_t(tiles) * 4 + 15) & ~size_t(15)) + size_t(tiles);
+}
+
+template <int C>
+TileList tile_list(const SplatArgs& a, int tiles) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(a.saved + size_t(3 * (C + 1) + 1) * a.P);
+  TileList t;
+  t.count = reinterpret_cast<unsigned*>(p);
+  t.list = reinterpret_cast<int*>(p + kListHeader);
+  t.flag = p + kListHeader + ((size_t(tiles) * 4 + 15) & ~size_t(15));
+  return t;
+}
+
+// Resident blocks per SM x SMs of a persistent kernel (host-side queries,
+// once per kernel and shared-memory size).
+template <typename K>
+int persistent_grid(K kern, size_t smem, size_t& cached_smem, int& cached_grid) {
+  if (cached_smem != smem || cached_grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTX * kTY, smem);
+    cached_grid = std::max(1, sms * std::max(1, per_sm));
+    cached_smem = smem;
+  }
+  return cached_grid;
+}
+
+template <typename K>
+bool reserve_smem(K kern, size_t smem, size_t& reserved, std::string& err) {
+  if (smem > 48 * 1024 && smem > reserved) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem)) != cudaSuccess) {
+      err = "layers x channels need more shared memory than the device has";
+      return false;
+    }
+    reserved = smem;
+  }
+  return true;
+}
+
+// With saved accumulators and a depth buffer (the training path) a call is
+// split: a light kernel classifies the tiles (forward) or zeros the
+// gradients of the empty ones (backward), and the heavy kernel runs
+// persistent blocks over the listed tiles only. Otherwise one block per
+// tile.
 template <int C, int LT>
 int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
               cudaStream_t stream, std::string& err) {
   const size_t smem = bwd ? bwd_smem(a.L, C) : fwd_smem(a.L, C);
   auto kern = bwd ? splat_bwd_kernel<C, LT> : splat_fwd_kernel<C, LT>;
+  auto list_kern = bwd ? splat_bwd_list_kernel<C, LT> : splat_fwd_list_kernel<C, LT>;
   // Raise the dynamic shared-memory limit once per kernel and size (host-side
   // attribute only; later calls skip it).
-  static size_t reserved[2] = {0, 0};
-  if (smem > 48 * 1024 && smem > reserved[bwd]) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem)) != cudaSuccess) {
-      err = "layers x channels need more shared memory than the device has";
-      return DR_ERR_INVALID_ARGUMENT;
-    }
-    reserved[bwd] = smem;
-  }
+  static size_t reserved[2] = {0, 0}, reserved_list[2] = {0, 0};
+  static size_t grid_smem[2] = {0, 0};
+  static int grid_blocks[2] = {0, 0};
+  if (!reserve_smem(kern, smem, reserved[bwd], err) ||
+      !reserve_smem(list_kern, smem, reserved_list[bwd], err))
+    return DR_ERR_INVALID_ARGUMENT;
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
     const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
     Batch b;
     if (!make_batch(images + g0, cnt, a.L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
     const int tiles = b.tile_start[cnt];
-    if (tiles > 0) kern<<<tiles, kTX * kTY, smem, stream>>>(a, b);
+    if (tiles <= 0) continue;
+    const bool listed = a.saved && a.zb && !a.accum && !a.normalized &&
+                        n <= DR_MAX_BATCH_INLINE && list_bytes(tiles) <= size_t(a.P) * 4;
+    if (!listed) {
+      kern<<<tiles, kTX * kTY, smem, stream>>>(a, b);
+      continue;
+    }
+    const TileList t = tile_list<C>(a, tiles);
+    const int grid = std::min(tiles, persistent_grid(list_kern, smem, grid_smem[bwd],
+                                                     grid_blocks[bwd]));
+    const unsigned light = unsigned((tiles + 7) / 8);
+    if (!bwd) {
+      if (cudaMemsetAsync(t.count, 0, kListHeader, stream) != cudaSuccess) {
+        err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(cudaGetLastError());
+        return DR_ERR_CUDA;
+      }
+      splat_classify_kernel<C><<<light, 256, 0, stream>>>(a, b, t, tiles);
+    } else {
+      splat_bwd_zero_kernel<C><<<light, 256, 0, stream>>>(a, b, t, tiles);
+    }
+    list_kern<<<grid, kTX * kTY, smem, stream>>>(a, b, t);
   }
   return launch_status(bwd ? "splat backward" : "splat", err);
 }

@@ -765,13 +765,14 @@ class _Splat(torch.autograd.Function):
     P = batch.total_pixels
     out = torch.empty(P, C, dtype=torch.float32, device=dev)
     needs_grad = positions.requires_grad or colors.requires_grad
-    saved = (torch.empty(3 * (C + 1) + 1, P, dtype=torch.float32, device=dev)
+    saved = (torch.empty(3 * (C + 1) + 2, P, dtype=torch.float32, device=dev)
              if needs_grad else None)
     accum = norm = None
     if want_accum:
       accum = torch.empty(3 * P, C, dtype=torch.float32, device=dev)
       norm = torch.empty_like(accum)
-    with _op("splat_fwd", _groups(batch)):
+    with _op("splat_fwd", _splat_launches(batch, saved is not None and z is not None and
+                                          not want_accum)):
       rc = lib.dr_splat_fwd(_p(positions), _p(z), _p(colors), C, batch.ptr, batch.n, L,
                             _p(out), _p(saved), _p(accum), _p(norm), _stream(dev))
     _lib.check(rc, "dr_splat_fwd")
@@ -810,13 +811,25 @@ class _Splat(torch.autograd.Function):
       d_out = d_out.clone()
     d_colors = torch.empty_like(colors)
     d_pos = torch.empty_like(positions)
-    with _op("splat_bwd", _groups(ctx.batch)):
+    with _op("splat_bwd", _splat_launches(ctx.batch, z is not None)):
       rc = lib.dr_splat_bwd(_p(d_out), _p(positions), _p(z), _p(colors), _p(saved),
                             colors.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L,
                             _p(d_colors), _p(d_pos), _stream(d_out.device))
     _lib.check(rc, "dr_splat_bwd")
     return (d_pos if ctx.needs_input_grad[0] else None,
             d_colors if ctx.needs_input_grad[1] else None, None, None, None, None)
+
+
+def _splat_launches(batch, listed):
+  """Kernels one splat call launches: with saved accumulators and a depth
+  buffer (and a batch of at most DR_MAX_BATCH_INLINE images whose tile list
+  fits its plane) a classifying (or zeroing) kernel plus the kernel over the
+  listed tiles, else one kernel per group of images."""
+  if listed and batch.n <= _lib.DR_MAX_BATCH_INLINE:
+    tiles = sum(((w + 31) // 32) * ((h + 7) // 8) for w, h in zip(batch.widths, batch.heights))
+    if 16 + ((4 * tiles + 15) & ~15) + tiles <= 4 * batch.total_pixels:
+      return 2
+  return _groups(batch)
 
 
 def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False, z=None):

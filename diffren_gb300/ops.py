@@ -50,7 +50,7 @@ def _(clip_vertices, triangles, width, height, num_layers, face_culling_mode, de
 @torch.library.custom_op(_NS + "::splat_fwd", mutates_args=())
 def splat_fwd(positions: torch.Tensor, colors: torch.Tensor,
               z_buffer: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
-  """(image [H, W, C], saved accumulators and surface codes [3 (C + 1) + 1, H * W])."""
+  """(image [H, W, C], saved accumulators, surface codes and tile list [3 (C + 1) + 2, H * W])."""
   L, H, W, C = colors.shape
   lib = _lib.load()
   batch = _single(W, H)
@@ -58,7 +58,7 @@ def splat_fwd(positions: torch.Tensor, colors: torch.Tensor,
   col = colors.reshape(-1, C).contiguous()
   z = z_buffer.reshape(-1).contiguous()
   out = torch.empty(H, W, C, dtype=torch.float32, device=colors.device)
-  saved = torch.empty(3 * (C + 1) + 1, H * W, dtype=torch.float32, device=colors.device)
+  saved = torch.empty(3 * (C + 1) + 2, H * W, dtype=torch.float32, device=colors.device)
   rc = lib.dr_splat_fwd(kernels._p(pos), kernels._p(z), kernels._p(col), C, batch.ptr, 1, L,
                         kernels._p(out), kernels._p(saved), None, None,
                         kernels._stream(colors.device))
@@ -69,7 +69,7 @@ def splat_fwd(positions: torch.Tensor, colors: torch.Tensor,
 @splat_fwd.register_fake
 def _(positions, colors, z_buffer):
   L, H, W, C = colors.shape
-  return colors.new_empty((H, W, C)), colors.new_empty((3 * (C + 1) + 1, H * W))
+  return colors.new_empty((H, W, C)), colors.new_empty((3 * (C + 1) + 2, H * W))
 
 
 @torch.library.custom_op(_NS + "::splat_bwd", mutates_args=())

@@ -394,12 +394,13 @@ int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
  * them unwritten; without it every position is read and its w is the
  * foreground flag. colors [L, H, W, C]
  * (1 <= C <= DR_MAX_SPLAT_CHANNELS, last channel alpha); out [H, W, C].
- * saved [3 (C + 1) + 1, P] receives the fg/surface/bg accumulators and
+ * saved [3 (C + 1) + 2, P] receives the fg/surface/bg accumulators and
  * weights the VJP needs, one plane of P pixels per value, P = the largest
- * pixel_offset + width * height of the images, and in its last plane (for
- * three layers) each pixel's surface classes of its 9 taps as 32-bit codes
- * (nullable; written only near foreground samples, where dr_splat_bwd reads
- * it); accum and normalized [3, H, W, C] are
+ * pixel_offset + width * height of the images, then (for three layers) each
+ * pixel's surface classes of its 9 taps as 32-bit codes, then the list of
+ * the screen tiles that hold foreground (nullable; the planes are written
+ * only near foreground samples, where dr_splat_bwd reads them); accum and
+ * normalized [3, H, W, C] are
  * the reference's debugging buffers (nullable). With C % 4 == 0 the color
  * and output buffers must be 16-byte aligned. */
 int dr_splat_fwd(const float* positions, const float* z_buffer, const float* colors,
@@ -410,7 +411,9 @@ int dr_splat_fwd(const float* positions, const float* z_buffer, const float* col
 /* VJP in gather form: each sample reads the adjoints of the 9 pixels it
  * reached (no atomics). Writes d_colors [L, H, W, C] and d_positions
  * [L, H, W, 4] as (d x, d y, 0, 0); with a z_buffer, d_positions of
- * background samples are left unwritten. `saved` is the forward's. */
+ * background samples are left unwritten. `saved` is the forward's; with a
+ * z_buffer the call resets a work counter kept in its last plane, so
+ * backward calls on one saved buffer must not overlap on the GPU. */
 int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buffer,
                  const float* colors, const float* saved, int32_t num_channels,
                  const dr_image_desc* images, int32_t num_images, int32_t num_layers,

@@ -18,7 +18,7 @@ def test_ops_are_registered_with_fake_shapes():
     assert z.shape == (3, 6, 8) and bary.shape == (3, 6, 8, 3)
     pos, col, zb = torch.empty(3, 6, 8, 4), torch.empty(3, 6, 8, 4), torch.empty(3, 6, 8)
     out, saved = torch.ops.diffren_gb300.splat_fwd(pos, col, zb)
-    assert out.shape == (6, 8, 4) and saved.shape == (16, 48)
+    assert out.shape == (6, 8, 4) and saved.shape == (17, 48)
     d_pos, d_col = torch.ops.diffren_gb300.splat_bwd(out, pos, col, zb, saved)
     assert d_pos.shape == pos.shape and d_col.shape == col.shape
 

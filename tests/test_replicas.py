@@ -72,9 +72,9 @@ def test_kernel_bytes_formulas():
   S = 3000
   b = bench.kernel_bytes(wl, fg=400, near=600, C=4, K=4)
   assert b["raster"] == 50 * 12 + 30 * 32 + S * 36 + 16 * 400
-  assert b["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 60 * 600
-  assert b["splat_bwd"] == 600 * 76 + 4 * S + 32 * 400 + 16 * S + 16 * 400
+  assert b["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 64 * 600
+  assert b["splat_bwd"] == 600 * 80 + 4 * S + 32 * 400 + 16 * S + 16 * 400
   assert b["samples_bwd"] == 4 * S + 400 * 64 + 30 * 32 * 3
   assert b["squared_error"] == 48 * 1000
   # near defaults to every pixel
-  assert bench.kernel_bytes(wl, fg=400)["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 60 * 1000
+  assert bench.kernel_bytes(wl, fg=400)["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 64 * 1000
