@@ -139,7 +139,7 @@ class BatchRenderer:
                                                                self.triangles, ids, z, b, L)
       else:
         interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
-    split = torch.split(interp, widths, dim=1)
+    split = kernels.split_channels(interp, widths, dim=1)
     shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
     shaded = shaded.reshape(-1, shaded.shape[-1])
     if splatting:

@@ -77,4 +77,4 @@ def interpolate_vertex_attributes(attributes: Dict[str, torch.Tensor],
   out = kernels.interpolate_packed(cat, bary, tris, ids, z, batch,
                                    framebuffer.num_layers, bg)
   out = _reshape_like(framebuffer, out)
-  return dict(zip(keys, torch.split(out, widths, dim=-1)))
+  return dict(zip(keys, kernels.split_channels(out, widths)))

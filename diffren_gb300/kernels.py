@@ -820,6 +820,15 @@ class _Splat(torch.autograd.Function):
             d_colors if ctx.needs_input_grad[1] else None, None, None, None, None)
 
 
+def split_channels(t, widths, dim=-1):
+  """The per-attribute views of a packed [.., sum(widths)] tensor. One
+  attribute is the tensor itself: torch.split's backward would copy the
+  whole gradient to concatenate a single piece."""
+  if len(widths) == 1:
+    return (t,)
+  return torch.split(t, list(widths), dim=dim)
+
+
 def _splat_launches(batch, listed):
   """Kernels one splat call launches: with saved accumulators and a depth
   buffer (and a batch of at most DR_MAX_BATCH_INLINE images whose tile list

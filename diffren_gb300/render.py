@@ -64,7 +64,7 @@ def _render_fused(geom, attributes, shading_function, num_layers, face_culling_m
   frame = rasterize.framebuffer_of(geom, num_layers, ids, z, bary)
   lead = (geom.B,) if geom.batched else ()
   interp = interp.view(*lead, num_layers, frame.height, frame.width, -1)
-  interpolated = dict(zip(keys, torch.split(interp, widths, dim=-1)))
+  interpolated = dict(zip(keys, kernels.split_channels(interp, widths)))
   shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
   return splat.splat_positions(vp, frame, shaded, return_accum_buffers)
 
