@@ -353,6 +353,17 @@ __device__ __forceinline__ uint32_t discretize_z(float z) {
   if (mag == 0) return 2147483647u;  // (0 + 1) * S
   const bool neg = bits >> 31;
   const int bexp = int(mag >> 23);
+  if (bexp >= 120 && bexp <= 126) {
+    // 2^-7 <= |z| < 1 (every visible depth but those near 0): the same
+    // computation as below with sh = 24..30, where N < 2^31 and P < 2^62
+    // fit 32- and 64-bit integers.
+    const int sh = 150 - bexp;
+    const uint32_t m = (mag & 0x7fffffu) | 0x800000u;
+    const uint32_t n = neg ? (1u << sh) - m : (1u << sh) + m;
+    const uint64_t P = uint64_t(n) * 2147483647u;
+    const uint64_t frac_mask = (1ull << sh) - 1;
+    if ((P & frac_mask) < frac_mask + 1 - (1ull << (sh - 22))) return uint32_t(P >> sh);
+  }
   const uint64_t M = bexp ? ((mag & 0x7fffffu) | 0x800000u) : (mag & 0x7fffffu);
   const int E = bexp ? bexp - 150 : -149;  // |z| = M * 2^E
   uint64_t N;
@@ -387,6 +398,24 @@ __device__ __forceinline__ uint32_t discretize_z(float z) {
 // RN_float(r). Fixed point in units of 2^-83 (q >= 1/S has ulp >= 2^-83).
 __device__ __forceinline__ float undiscretize_z(uint32_t d) {
   const uint32_t S = 2147483647u;
+  if (d >= S && d < 2 * S) {
+    // q = d / S in [1, 2) (every depth in [0, 1)): with e = d - S and
+    // T = e (2^31 + 1), floor(e / S * 2^93) / 2^41 = e 2^21 + T / 2^41, so
+    // RN_double(q) - 1 = R 2^-52 with R = e 2^21 + T >> 41 + bit 40 of T
+    // (the remainder is never zero, so there are no ties), exact in double;
+    // then R rounds to 24 bits, ties to even.
+    const uint64_t e = d - S;
+    const uint64_t T = (e << 31) + e;
+    const uint64_t R = (e << 21) + (T >> 41) + ((T >> 40) & 1u);
+    if (R == 0) return 0.0f;
+    const int bl = 64 - __clzll(R);
+    if (bl <= 24) return float(uint32_t(R)) * 0x1p-52f;
+    const int g = bl - 24;
+    uint64_t mant = R >> g;
+    const uint64_t rem = R & ((1ull << g) - 1), half = 1ull << (g - 1);
+    if (rem > half || (rem == half && (mant & 1))) ++mant;
+    return float(uint32_t(mant)) * __uint_as_float(uint32_t(127 + g - 52) << 23);
+  }
   const u128 one = 1;
   const uint32_t I = (d >= S) + (d >= 2 * S);
   const uint64_t e = d - uint64_t(I) * S;  // d / S = I + e / S, e < S
