@@ -153,7 +153,11 @@ __device__ __forceinline__ long long shl16(long long a) {
 
 // ToFixedPoint (rasterize_utils.h:57-59): 16 fractional bits.
 __device__ __forceinline__ long long to_fixed(float f) {
-  return __float2ll_rz(__fmul_rn(f, 65536.0f));
+  const float s = __fmul_rn(f, 65536.0f);
+  // Below 2^31 the 32-bit conversion truncates to the same value (NaN fails
+  // the test and takes the 64-bit conversion, which maps it to INT64_MIN).
+  if (fabsf(s) < 2147483648.0f) return (long long)__float2int_rz(s);
+  return __float2ll_rz(s);
 }
 
 // AddPoint (rasterize_utils.h:75-84) on the running box {l, r, b, t}.

@@ -56,9 +56,10 @@ struct RasterArgs {
   int32_t total_tiles;
   TriSetup* setup;
   int4* bbox;  // {left, right, bottom, top}; empty when culled
-  int32_t* tile_count;
-  int32_t* tile_fill;
-  int32_t* tile_first;  // exclusive scan of tile_count, total_tiles + 1
+  int32_t* tile_count;  // triangles inside one tile (their slots come from here)
+  int32_t* tile_multi;  // triangles spanning 2..large_tiles tiles
+  int32_t* tile_fill;   // bin slots taken by the multi-tile triangles
+  int32_t* tile_first;  // exclusive scan of tile_count + tile_multi, total_tiles + 1
   int32_t* bins;        // global triangle indices grouped by tile
   int32_t* large_count;  // per image
   int32_t* large_list;   // per image, at tri_start[image]
@@ -71,7 +72,7 @@ struct RasterArgs {
 
 // Workspace: the zeroed block first, then the rest; 256-byte aligned parts.
 struct Layout {
-  size_t counters, tile_count, tile_fill, large_count, zero_end;
+  size_t counters, tile_count, tile_multi, tile_fill, large_count, zero_end;
   size_t tile_first, setup, bbox, bins, large_list, total;
 };
 
@@ -82,6 +83,7 @@ Layout make_layout(int64_t tris, int64_t tiles, int images, int large_tiles) {
   size_t o = 0;
   l.counters = o; o = align_up(o + 64);  // [0] queue head, [1] error flags
   l.tile_count = o; o = align_up(o + 4 * tiles);
+  l.tile_multi = o; o = align_up(o + 4 * tiles);
   l.tile_fill = o; o = align_up(o + 4 * tiles);
   l.large_count = o; o = align_up(o + 4 * size_t(images));
   l.zero_end = o;
@@ -181,13 +183,19 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
   const int tile0 = base + ty0 * tx + tx0;
   const unsigned group = __match_any_sync(0xffffffffu, single ? tile0 : -1 - lane);
   if (single) {
-    if (lane == __ffs(group) - 1) atomicAdd(&a.tile_count[tile0], __popc(group));
+    // The warp's triangles in this tile take consecutive slots; the slot is
+    // kept in the setup record, so the binning pass needs no atomic.
+    const int leader = __ffs(group) - 1;
+    int first = 0;
+    if (lane == leader) first = atomicAdd(&a.tile_count[tile0], __popc(group));
+    first = __shfl_sync(group, first, leader);
+    a.setup[g].pad[0] = first + __popc(group & ((1u << lane) - 1u));
     return;
   }
   if (!valid) return;
   if (n <= a.large_tiles) {
     for (int y = ty0; y <= ty1; ++y)
-      for (int x = tx0; x <= tx1; ++x) atomicAdd(&a.tile_count[base + y * tx + x], 1);
+      for (int x = tx0; x <= tx1; ++x) atomicAdd(&a.tile_multi[base + y * tx + x], 1);
   } else {
     const int slot = atomicAdd(&a.large_count[img], 1);
     a.large_list[B.tri_start[img] + slot] = int(g);
@@ -199,6 +207,7 @@ __global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
 // with coalesced loads and scanned with warp shuffles, then the 32 warp
 // totals are scanned once; the next pass's counts load meanwhile.
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
+                                                         const int32_t* multi,
                                                          int32_t* first, int n) {
   __shared__ int warp_sums[32];
   constexpr int kRounds = 16, kChunk = 1024 * kRounds;
@@ -209,7 +218,7 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
 #pragma unroll
     for (int j = 0; j < kRounds; ++j) {
       const int i = base + warp * (32 * kRounds) + j * 32 + lane;
-      dst[j] = i < n ? __ldg(count + i) : 0;
+      dst[j] = i < n ? __ldg(count + i) + __ldg(multi + i) : 0;
     }
   };
   load(0, v);
@@ -245,9 +254,6 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const int32_t* count,
 // box touches. Order inside a bin is irrelevant to the result.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B) {
   const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  // Every lane stays to the warp-wide match below; `binned` marks lanes
-  // with a triangle to bin.
   bool binned = false;
   int tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, base = 0, tx = 0;
   if (g < a.total_tris) {
@@ -262,25 +268,18 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B)
       }
     }
   }
-  // Triangles inside one tile (most of them, and neighbours in the mesh
-  // order) take their bin slots with one atomic per tile per warp.
-  const bool single = binned && tx0 == tx1 && ty0 == ty1;
-  const int tile0 = base + ty0 * tx + tx0;
-  const unsigned group = __match_any_sync(0xffffffffu, single ? tile0 : -1 - lane);
-  const int leader = __ffs(group) - 1;
-  int slot = 0;
-  if (single && lane == leader) slot = atomicAdd(&a.tile_fill[tile0], __popc(group));
-  slot = __shfl_sync(0xffffffffu, slot, leader);
-  if (single) {
-    const int rank = __popc(group & ((1u << lane) - 1u));
-    a.bins[a.tile_first[tile0] + slot + rank] = int(g);
+  // Triangles inside one tile (most of them) took their slot in setup;
+  // the multi-tile ones take theirs after the tile's single-tile triangles.
+  if (!binned) return;
+  if (tx0 == tx1 && ty0 == ty1) {
+    const int tile0 = base + ty0 * tx + tx0;
+    a.bins[a.tile_first[tile0] + a.setup[g].pad[0]] = int(g);
     return;
   }
-  if (!binned) return;
   for (int y = ty0; y <= ty1; ++y)
     for (int x = tx0; x <= tx1; ++x) {
       const int tile = base + y * tx + x;
-      const int pos = a.tile_first[tile] + atomicAdd(&a.tile_fill[tile], 1);
+      const int pos = a.tile_first[tile] + a.tile_count[tile] + atomicAdd(&a.tile_fill[tile], 1);
       a.bins[pos] = int(g);
     }
 }
@@ -421,8 +420,8 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
       if (i < TW) s.pxf[i] = pixel_center_fixed(x0 + i, W, disc);
       else s.pyf[i - TW] = pixel_center_fixed(y0 + i - TW, H, disc);
     }
-    const int nbin = a.tile_count[item];
     const int bin0 = a.tile_first[item];
+    const int nbin = a.tile_first[item + 1] - bin0;
     const int nlarge = a.large_count[img];
     const int nsrc = nbin + nlarge;
     __syncthreads();
@@ -847,6 +846,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     a.setup = reinterpret_cast<TriSetup*>(ws + lay.setup);
     a.bbox = reinterpret_cast<int4*>(ws + lay.bbox);
     a.tile_count = reinterpret_cast<int32_t*>(ws + lay.tile_count);
+    a.tile_multi = reinterpret_cast<int32_t*>(ws + lay.tile_multi);
     a.tile_fill = reinterpret_cast<int32_t*>(ws + lay.tile_fill);
     a.tile_first = reinterpret_cast<int32_t*>(ws + lay.tile_first);
     a.bins = reinterpret_cast<int32_t*>(ws + lay.bins);
@@ -866,7 +866,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
       const unsigned grid = unsigned((tris + 255) / 256);
       setup_kernel<<<grid, 256, 0, stream>>>(a, b);
     }
-    tile_scan_kernel<<<1, 1024, 0, stream>>>(a.tile_count, a.tile_first, tiles);
+    tile_scan_kernel<<<1, 1024, 0, stream>>>(a.tile_count, a.tile_multi, a.tile_first, tiles);
     if (tris > 0) {
       const unsigned grid = unsigned((tris + 255) / 256);
       bin_scatter_kernel<<<grid, 256, 0, stream>>>(a, b);

@@ -512,6 +512,18 @@ __device__ __forceinline__ void load_groups(const float* p, float4* g) {
   for (int q = 0; q < Q; ++q) g[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
+// Position of the (r + 1)-th set bit of m (r < popc(m)), by halving
+// (measured a little faster than __fns here).
+__device__ __forceinline__ int nth_set_bit(unsigned m, int r) {
+  int pos = 0, c;
+  c = __popc(m & 0xffffu); if (r >= c) { r -= c; pos += 16; m >>= 16; }
+  c = __popc(m & 0xffu); if (r >= c) { r -= c; pos += 8; m >>= 8; }
+  c = __popc(m & 0xfu); if (r >= c) { r -= c; pos += 4; m >>= 4; }
+  c = __popc(m & 0x3u); if (r >= c) { r -= c; pos += 2; m >>= 2; }
+  c = int(m & 1u); if (r >= c) pos += 1;
+  return pos;
+}
+
 struct TileRef {
   int img, x0, y0;
 };
@@ -657,7 +669,7 @@ __device__ __forceinline__ void splat_fwd_tile(const SplatArgs& a, const Batch& 
 #pragma unroll
           for (int ll = 1; ll < (LT > 0 ? LT : 1); ++ll)
             if (l == ll) ml = masks[ll];
-          const int src = __fns(ml, 0, r + 1);
+          const int src = nth_set_bit(ml, r);
           const int ii = wbase + src;
           const int ry = ii / kRS;
           const int x = tr.x0 - 1 + (ii - ry * kRS), y = tr.y0 - 1 + ry;
@@ -1116,7 +1128,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
 #pragma unroll
         for (int ll = 1; ll < kL; ++ll)
           if (l == ll) ml = masks[ll];
-        src = __fns(ml, 0, r + 1);
+        src = nth_set_bit(ml, r);
       }
       int ss[9];
 #pragma unroll
