@@ -60,6 +60,9 @@ def parse():
   ap.add_argument("--no-plain", action="store_true")
   ap.add_argument("--no-parity", action="store_true",
                   help="skip the CPU comparison of the first images and gradients")
+  ap.add_argument("--recompute-raster", action="store_true",
+                  help="the VJP reruns the rasterizer instead of keeping its ids, "
+                       "barycentrics and vertex ids (memory-tight mode)")
   ap.add_argument("--cpu-budget", type=float, default=20.0,
                   help="seconds of CPU work per reference-arm step / baseline")
   return ap.parse_args()
@@ -334,7 +337,8 @@ def run_ours(args, rank, world, device):
   wl = Workload(args.workload, args.num_meshes)
   r = batch_lib.BatchRenderer([m.triangles for m in wl.meshes],
                               [len(m.vertices) for m in wl.meshes], wl.sizes,
-                              num_layers=wl.num_layers, device=device, tile="auto")
+                              num_layers=wl.num_layers, device=device, tile="auto",
+                              recompute_raster=args.recompute_raster)
   from diffren_gb300 import shaders
   textured = wl.texture is not None
   verts_h = torch.from_numpy(np.concatenate([m.vertices for m in wl.meshes])).pin_memory()
@@ -379,8 +383,12 @@ def run_ours(args, rank, world, device):
   # Launch count of our kernels in one step (eager), and the step's results
   # on the first images for the parity check.
   kernels.LAUNCHES.reset()
+  torch.cuda.synchronize(device)
+  mem0 = torch.cuda.memory_allocated(device)
+  torch.cuda.reset_peak_memory_stats(device)
   res0 = step()
   torch.cuda.synchronize(device)
+  step_peak_bytes = torch.cuda.max_memory_allocated(device) - mem0
   launches_per_step = kernels.LAUNCHES.count
   gpu = None
   if rank == 0 and not args.no_parity:
@@ -501,7 +509,7 @@ def run_ours(args, rank, world, device):
   tile = [r.config.tile_width, r.config.tile_height, r.config.large_tiles]
   return dict(wl=wl, fg=fg, near=near, tile=tile, ms=ms, ms_e2e=ms_e2e, h2d=h2d, d2h=d2h, clock=clock,
               loss=loss_val, launches=launches_per_step, per_kernel=per_kernel,
-              plain=plain, renderer=r, gpu=gpu)
+              plain=plain, renderer=r, gpu=gpu, step_peak_bytes=step_peak_bytes)
 
 
 def run_plain(wl, device, args):
@@ -795,7 +803,9 @@ def main():
       "details": {"foreground_samples": res["fg"], "pixels_near_foreground": res["near"],
                   "parallelism": "replicas" if world > 1 else "1 GPU",
                   "cuda_graph": True, "raster_tile_autotuned": res["tile"],
-                  "depth_semantics": "discretized (the reference CUDA rasterizer's)"},
+                  "depth_semantics": "discretized (the reference CUDA rasterizer's)",
+                  "recompute_raster": bool(args.recompute_raster),
+                  "step_peak_device_bytes": res["step_peak_bytes"]},
       "parity": parity,
       "e2e": {"value": whole_job_mpix(world, wl.pixels, res["ms_e2e"]), "unit": "Mpix/s",
               "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},

@@ -23,7 +23,8 @@ namespace {
 
 // Fine-raster block = triangle chunk size. 128-thread blocks keep eight
 // tiles in flight per SM (each tile's setup, scan and epilogue are serial
-// latency chains), which measured faster than four 256-thread tiles.
+// latency chains), which measured faster than four 256-thread tiles and
+// than sixteen 64-thread ones.
 constexpr int kThreads = 128;
 constexpr int kDefaultTile = 16;
 constexpr int kDefaultLargeTiles = 16;
@@ -297,13 +298,20 @@ struct FineSmem {
   long long* pxf;        // [TW] fixed-point pixel-center x
   long long* pyf;        // [TH]
   unsigned long long* keys;  // [L][TW*TH]
-  unsigned char* first;  // [8 * TW*TH] slot holding candidate 32 g, per g
+  unsigned char* first;  // [kThreads / 32 * TW*TH] slot holding candidate 32 g, per g
 };
 
+// The chunk's edge coefficients; the epilogue reuses the space for its list
+// of occupied (layer, pixel) slots (16 bits each).
+__host__ __device__ inline size_t chunk_m_bytes(int L, int TW, int TH) {
+  const size_t m = size_t(9) * kThreads * 8, list = size_t(L) * TW * TH * 2;
+  return ((m > list ? m : list) + 7) & ~size_t(7);
+}
+
 __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
-  return size_t(9) * kThreads * 8 + size_t(TW + TH) * 8 +
+  return chunk_m_bytes(L, TW, TH) + size_t(TW + TH) * 8 +
          size_t(L) * TW * TH * 8 + size_t(6) * kThreads * 4 +
-         size_t(4) * kThreads * 4 + 16 + size_t(8) * TW * TH + 64;
+         size_t(4) * kThreads * 4 + 16 + size_t(kThreads / 32) * TW * TH + 64;
 }
 
 // Persistent fine rasterizer. Each block takes (image, tile) items from a
@@ -388,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
   {
     unsigned char* p = smem_raw;
     s.keys = reinterpret_cast<unsigned long long*>(p); p += size_t(L) * TP * 8;
-    s.m = reinterpret_cast<long long*>(p); p += size_t(9) * kThreads * 8;
+    s.m = reinterpret_cast<long long*>(p); p += chunk_m_bytes(L, TW, TH);
     s.pxf = reinterpret_cast<long long*>(p); p += size_t(TW) * 8;
     s.pyf = reinterpret_cast<long long*>(p); p += size_t(TH) * 8;
     s.vz = reinterpret_cast<float*>(p); p += size_t(3) * kThreads * 4;
