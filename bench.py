@@ -5,7 +5,10 @@ icospheres or triangle soups, 50/50), triangle counts lognormal (median 20k,
 sigma 1.2) clipped to [500, 500k], one camera per mesh on a sphere of radius
 3, square resolutions drawn from {256, 512, 1024}, 3 depth layers, back-face
 culling, RGBA vertex colors (RGB seeded, alpha 1) interpolated as an
-attribute and passed through by the deferred shader. One step = forward
+attribute and used as the splat colors (shading_function=None, the
+pass-through `lambda a: a['rgba']` of the reference's render tests, under
+which background samples' attributes and color gradients are not written;
+both arms render this way). One step = forward
 render of every image + L2 loss against fixed target images + backward to
 vertex positions and vertex colors (the optimized color parameter is the
 RGBA vertex color; the RGB gradients are its first three columns).
@@ -127,10 +130,9 @@ class Workload:
       t[..., 3] = 1.0
 
 
-def shader(a):
-  """Pass-through of the interpolated RGBA vertex colors (the reference's
-  render tests shade with `lambda x: x['rgba']` the same way)."""
-  return a["rgba"]
+# Pass-through of the interpolated RGBA vertex colors (the reference's
+# render tests shade with `lambda x: x['rgba']`): the renderers' None.
+shader = None
 
 
 LIGHT = (2.0, 2.0, 2.0)
@@ -274,30 +276,37 @@ TRAFFIC_PER_SAMPLE = {"raster": 44.3, "splat_fwd": 24.48, "splat_bwd": 43.46,
                       "samples_bwd": 23.15}
 
 
-def kernel_bytes(wl, fg, near=None, C=4, K=4):
+def kernel_bytes(wl, fg, near=None, C=4, K=4, passthrough=False, vids=True):
   """Algorithmic (compulsory) HBM bytes per launch of each kernel: every
   input read and every output written once. `fg` = foreground layer samples
   among the L * P; work on background samples stops after their depth.
   `near` = pixels within one pixel of a foreground sample (the only ones
-  whose splat accumulators the backward needs); all pixels if None."""
+  whose splat accumulators the backward needs); all pixels if None.
+  `passthrough`: the splat colors are the interpolated attributes
+  (shading_function None), so background attributes and color gradients
+  are not written. `vids`: the rasterizer stores vertex ids (no
+  recompute)."""
   L, P, T, V = wl.num_layers, wl.pixels, wl.triangles, wl.vertices
   S = L * P
   near = P if near is None else near
+  written = fg if passthrough else S  # samples whose attributes / d colors are written
   return {
       # rasterizer with the fused interpolation epilogue: the mesh (indices,
-      # clip vertices, attributes) in; ids, z, bary and K attributes of
-      # every sample and the viewport position of every foreground sample out
-      "raster": T * 12 + V * (16 + 4 * K) + S * (20 + 4 * K) + 16 * fg,
+      # clip vertices, attributes) in; z of every sample, ids, barycentrics,
+      # viewport position (and vertex ids) of every foreground sample and K
+      # attributes of the written samples out
+      "raster": (T * 12 + V * (16 + 4 * K) + 4 * S + fg * (16 + 16 + (12 if vids else 0))
+                 + 4 * K * written),
       # depth of every sample, position and color of every foreground
       # sample in; composited color per pixel, saved accumulators (3 (C + 1))
       # and the surface code per pixel near foreground out
       "splat_fwd": 4 * S + (16 + 4 * C) * fg + 4 * C * P + (12 * (C + 1) + 4) * near,
       # saved accumulators, surface code and d color per pixel near
       # foreground, depth of every sample, position and color of the
-      # foreground ones in; d color of every sample and d position of every
-      # foreground sample out
-      "splat_bwd": (near * (12 * (C + 1) + 4 + 4 * C) + 4 * S + (16 + 4 * C) * fg + 4 * C * S
-                    + 16 * fg),
+      # foreground ones in; d color of the written samples and d position of
+      # every foreground sample out
+      "splat_bwd": (near * (12 * (C + 1) + 4 + 4 * C) + 4 * S + (16 + 4 * C) * fg
+                    + 4 * C * written + 16 * fg),
       # z of every sample; ids, bary, d position and d attributes of the
       # depth of every sample; barycentrics, vertex indices, d position,
       # position and d attributes of the foreground ones; vertex gradients
@@ -789,7 +798,9 @@ def main():
     return
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
-  nbytes = kernel_bytes(wl, res["fg"], res["near"], K=2 if wl.texture is not None else 4)
+  nbytes = kernel_bytes(wl, res["fg"], res["near"], K=2 if wl.texture is not None else 4,
+                        passthrough=wl.texture is None and not wl.lit,
+                        vids=not args.recompute_raster)
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9
   value = whole_job_mpix(world, wl.pixels, res["ms"])

@@ -16,6 +16,8 @@ DR_DEPTH_DISCRETIZED, DR_DEPTH_FLOAT = 0, 1
 DR_FLAG_INDEX_OUT_OF_RANGE = 1
 DR_FLAG_NONFINITE_VERTEX = 2
 DR_RASTER_FOREGROUND_ONLY = 1
+DR_RASTER_FOREGROUND_ATTRIBUTES = 2
+DR_SPLAT_FOREGROUND_GRADIENTS = 1
 DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
@@ -88,6 +90,8 @@ SIGNATURES = {
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
     "dr_splat_jvp": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_splat_bwd": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),
+    "dr_splat_bwd_ex": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, ctypes.c_uint32, _P, _P,
+                             _P]),
 }
 
 _lib = None

@@ -101,6 +101,10 @@ class BatchRenderer:
 
     vertices [sum V, 3|4] packed per mesh; attributes: dict of [sum V, K];
     cameras [N, 4, 4] (one per image) or None for clip-space vertices.
+    ``shading_function`` None (beyond the reference's arguments): the single
+    attribute is the color, as ``lambda a: a[key]`` gives; with splatting
+    the background samples' attributes and color gradients, which nothing
+    then reads, are not written.
     """
     if (compositing_mode == constants.CompositingMode.SPLAT_OVER and
         self.face_culling_mode != constants.FaceCullingMode.BACK):
@@ -117,6 +121,9 @@ class BatchRenderer:
                                torch.as_tensor(cameras, device=self.device), b)
     L = self.num_layers
     keys = list(attributes.keys())
+    passthrough = shading_function is None
+    if passthrough and len(keys) != 1:
+      raise ValueError("shading_function=None needs exactly one attribute")
     parts = [kernels._f32(attributes[k], self.device) for k in keys]
     widths = [p.shape[1] for p in parts]
     cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0]
@@ -129,8 +136,11 @@ class BatchRenderer:
       # the splat positions of every layer sample.
       # The splat path tells background samples by the depth buffer, so
       # their ids and barycentrics need not be written.
+      # A pass-through shader leaves the splat the only reader of the
+      # attributes: background rows need not be written either.
       interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
-          cat, clip, self.triangles, b, kernels.foreground_only(self.config), self.workspace,
+          cat, clip, self.triangles, b,
+          kernels.foreground_only(self.config, attributes=passthrough), self.workspace,
           self.recompute_raster)
     else:
       ids, z, bary = self.rasterize(clip)
@@ -139,11 +149,15 @@ class BatchRenderer:
                                                                self.triangles, ids, z, b, L)
       else:
         interp = kernels.interpolate_packed(cat, bary, self.triangles, ids, z, b, L)
-    split = kernels.split_channels(interp, widths, dim=1)
-    shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
-    shaded = shaded.reshape(-1, shaded.shape[-1])
+    if passthrough:
+      shaded = interp
+    else:
+      split = kernels.split_channels(interp, widths, dim=1)
+      shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
+      shaded = shaded.reshape(-1, shaded.shape[-1])
     if splatting:
-      return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers, z=z)
+      return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers, z=z,
+                                  foreground_gradients=passthrough and fused)
     if compositing_mode == constants.CompositingMode.NONE:
       return shaded * (z != 1.0).float()[:, None]
     return kernels.over_packed(shaded, z, b, L)

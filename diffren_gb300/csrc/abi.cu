@@ -52,7 +52,7 @@ extern "C" {
 
 const char* dr_last_error(void) { return g_error.c_str(); }
 
-int32_t dr_abi_version(void) { return 2; }
+int32_t dr_abi_version(void) { return 3; }
 
 size_t dr_rasterize_batch_workspace_bytes(const dr_image_desc* images,
                                           int32_t num_images,
@@ -342,15 +342,23 @@ int dr_splat_fwd(const float* positions, const float* z_buffer, const float* col
                 err);
 }
 
+int dr_splat_bwd_ex(const float* d_out, const float* positions, const float* z_buffer,
+                    const float* colors, const float* saved, int32_t num_channels,
+                    const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                    uint32_t flags, float* d_colors, float* d_positions, void* stream) {
+  std::string err;
+  return finish(dr::splat_bwd_launch(d_out, positions, z_buffer, colors, saved, num_channels,
+                                     images, num_images, num_layers, flags, d_colors,
+                                     d_positions, as_stream(stream), err),
+                err);
+}
+
 int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buffer,
                  const float* colors, const float* saved, int32_t num_channels,
                  const dr_image_desc* images, int32_t num_images, int32_t num_layers,
                  float* d_colors, float* d_positions, void* stream) {
-  std::string err;
-  return finish(dr::splat_bwd_launch(d_out, positions, z_buffer, colors, saved, num_channels,
-                                     images, num_images, num_layers, d_colors, d_positions,
-                                     as_stream(stream), err),
-                err);
+  return dr_splat_bwd_ex(d_out, positions, z_buffer, colors, saved, num_channels, images,
+                         num_images, num_layers, 0u, d_colors, d_positions, stream);
 }
 
 int dr_splat_jvp(const float* positions, const float* z_buffer, const float* colors,

@@ -159,7 +159,8 @@ int splat_jvp_launch(const float* positions, const float* z_buffer, const float*
                      cudaStream_t stream, std::string& err);
 int splat_bwd_launch(const float* d_out, const float* positions, const float* z_buffer,
                      const float* colors, const float* saved, int C,
-                     const dr_image_desc* images, int n, int L, float* d_colors,
-                     float* d_positions, cudaStream_t stream, std::string& err);
+                     const dr_image_desc* images, int n, int L, uint32_t flags,
+                     float* d_colors, float* d_positions, cudaStream_t stream,
+                     std::string& err);
 
 }  // namespace dr

@@ -53,6 +53,7 @@ struct RasterArgs {
   const int32_t* tris;
   int culling, depth_mode, L, TW, TH, large_tiles;
   bool fg_only;  // DR_RASTER_FOREGROUND_ONLY: background ids / barycentrics unwritten
+  bool fg_attr;  // DR_RASTER_FOREGROUND_ATTRIBUTES: background attributes unwritten
   int64_t total_tris;
   int32_t total_tiles;
   TriSetup* setup;
@@ -374,7 +375,7 @@ __device__ __forceinline__ void write_sample(const RasterArgs& a, const Batch& B
       vo[1] = v1;
       vo[2] = v2;
     }
-  } else if (ao) {
+  } else if (ao && !a.fg_attr) {
     // Background: attributes 0; the position is left unwritten (consumers
     // take background samples from the depth buffer).
     for (int k = 0; k < K; k += 4)
@@ -747,7 +748,7 @@ bool check_config(const dr_raster_config* cfg, int& L, int& TW, int& TH, int& la
     err = "tile must satisfy width, height <= 128 and width*height <= 1024";
     return false;
   }
-  if ((cfg->flags & ~DR_RASTER_FOREGROUND_ONLY) != 0) {
+  if ((cfg->flags & ~(DR_RASTER_FOREGROUND_ONLY | DR_RASTER_FOREGROUND_ATTRIBUTES)) != 0) {
     err = "unknown raster config flags";
     return false;
   }
@@ -848,6 +849,7 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     a.culling = cfg->face_culling_mode;
     a.depth_mode = cfg->depth_mode;
     a.fg_only = (cfg->flags & DR_RASTER_FOREGROUND_ONLY) != 0;
+    a.fg_attr = (cfg->flags & DR_RASTER_FOREGROUND_ATTRIBUTES) != 0;
     a.L = L; a.TW = TW; a.TH = TH; a.large_tiles = large;
     a.total_tris = tris;
     a.total_tiles = tiles;

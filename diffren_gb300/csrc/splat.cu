@@ -426,6 +426,7 @@ struct SplatArgs {
   const float* d_out;
   float* d_colors;
   float4* d_vp;
+  bool fg_grads;  // DR_SPLAT_FOREGROUND_GRADIENTS: background d_colors unwritten
 };
 
 // A block covers a kTX x kTY tile of pixels, one per thread; the samples it
@@ -759,7 +760,9 @@ __device__ __forceinline__ void splat_fwd_tile(const SplatArgs& a, const Batch& 
       const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
       const int s = p - v * kRS - u;
       const unsigned m = in ? (wide ? unsigned(fgm16[s]) : unsigned(fgm8[s])) : 0u;
-      tap[j] = m ? m | (unsigned(surface_index(zs, s, p, L) + 16) << 16) : 0u;
+      // The center tap (s == p) always has surface index 0: both argmins
+      // start at a zero (or NaN) difference that no layer beats.
+      tap[j] = m ? m | (unsigned((j == 4 ? 0 : surface_index(zs, s, p, L)) + 16) << 16) : 0u;
       // Surface index + 2 in 3 bits per tap (three layers: -2..2) for the
       // VJP, which then needs no depths.
       if (LT == 3 && tap[j]) code |= ((tap[j] >> 16) - 14u) << (3 * j);
@@ -1014,7 +1017,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
     }
   }
   if (!__syncthreads_or(own != 0)) {
-    if (mine) {
+    if (mine && !a.fg_grads) {
       float dc[4 * Q];
 #pragma unroll
       for (int c = 0; c < 4 * Q; ++c) dc[c] = 0.0f;
@@ -1098,7 +1101,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
                             (3 * j)) & 7u) - 2
                      : 0;
       else
-        surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
+        surf[j] = in && j != 4 ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;  // center: 0
     }
     constexpr int kL = LT > 0 ? LT : 1;
     unsigned masks[kL];
@@ -1106,7 +1109,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
 #pragma unroll
     for (int l = 0; l < kL; ++l) {
       const bool fg = mine && ((own >> l) & 1u);
-      if (mine && !fg) {
+      if (mine && !fg && !a.fg_grads) {
         float dz[4 * Q];
 #pragma unroll
         for (int c = 0; c < 4 * Q; ++c) dz[c] = 0.0f;
@@ -1169,7 +1172,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
     const int px = sx + u, py = sy + v;
     const bool in = px >= 0 && py >= 0 && px < W && py < H;
     ok |= unsigned(in) << j;
-    surf[j] = in ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;
+    surf[j] = in && j != 4 ? surface_index(zs, s1, s1 + v * kRS + u, L) : 0;  // center: 0
   }
   for (int l = 0; l < L; ++l) {
     const int64_t e = ebase + l * HW;
@@ -1191,7 +1194,7 @@ __device__ __forceinline__ void splat_bwd_tile(const SplatArgs& a, const Batch& 
       dc[2 * hh] = dcol[hh].x;
       dc[2 * hh + 1] = dcol[hh].y;
     }
-    store_row<C>(a.d_colors + e * C, dc);
+    if (fgw != 0.0f || !a.fg_grads) store_row<C>(a.d_colors + e * C, dc);
     if (fgw != 0.0f || !a.zb) a.d_vp[e] = make_float4(dvx, dvy, 0.0f, 0.0f);
   }
 }
@@ -1230,7 +1233,7 @@ __global__ void __launch_bounds__(256) splat_bwd_zero_kernel(SplatArgs a, Batch 
                                                              int tiles) {
   if (blockIdx.x == 0 && threadIdx.x == 0) t.count[2] = 0u;
   const int item = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (item >= tiles || t.flag[item]) return;
+  if (a.fg_grads || item >= tiles || t.flag[item]) return;
   const int lane = threadIdx.x & 31;
   const TileRef tr = tile_at(B, item);
   const int W = B.width[tr.img], H = B.height[tr.img];
@@ -1714,11 +1717,19 @@ int splat_fwd_launch(const float* positions, const float* z_buffer, const float*
 
 int splat_bwd_launch(const float* d_out, const float* positions, const float* z_buffer,
                      const float* colors, const float* saved, int C,
-                     const dr_image_desc* images, int n, int L,
+                     const dr_image_desc* images, int n, int L, uint32_t flags,
                      float* d_colors, float* d_positions, cudaStream_t stream,
                      std::string& err) {
   int rc;
   if (!check_batch(L, n, images, err, rc)) return rc;
+  if ((flags & ~DR_SPLAT_FOREGROUND_GRADIENTS) != 0) {
+    err = "unknown splat flags";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  if ((flags & DR_SPLAT_FOREGROUND_GRADIENTS) && !z_buffer) {
+    err = "DR_SPLAT_FOREGROUND_GRADIENTS needs the depth buffer";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
   if (!saved) {
     err = "splat backward needs the accumulators saved by the forward pass";
     return DR_ERR_INVALID_ARGUMENT;
@@ -1739,6 +1750,7 @@ int splat_bwd_launch(const float* d_out, const float* positions, const float* z_
   a.saved = const_cast<float*>(saved);
   a.d_out = d_out; a.d_colors = d_colors;
   a.d_vp = reinterpret_cast<float4*>(d_positions);
+  a.fg_grads = (flags & DR_SPLAT_FOREGROUND_GRADIENTS) != 0;
   return dispatch(true, C, a, images, n, stream, err);
 }
 

@@ -174,11 +174,13 @@ def raster_config(num_layers, face_culling_mode, depth_mode, tile=(0, 0),
   return c
 
 
-def foreground_only(config):
-  """A copy of `config` with DR_RASTER_FOREGROUND_ONLY set."""
+def foreground_only(config, attributes=False):
+  """A copy of `config` with DR_RASTER_FOREGROUND_ONLY set (and, with
+  ``attributes``, DR_RASTER_FOREGROUND_ATTRIBUTES)."""
   return raster_config(config.num_layers, config.face_culling_mode, config.depth_mode,
                        (config.tile_width, config.tile_height), config.large_tiles,
-                       config.flags | _lib.DR_RASTER_FOREGROUND_ONLY)
+                       config.flags | _lib.DR_RASTER_FOREGROUND_ONLY |
+                       (_lib.DR_RASTER_FOREGROUND_ATTRIBUTES if attributes else 0))
 
 
 class Workspace:
@@ -758,7 +760,7 @@ def splat_positions_packed(clip, bary, triangles, ids, z, batch, num_layers):
 class _Splat(torch.autograd.Function):
 
   @staticmethod
-  def forward(ctx, positions, colors, z, batch, L, want_accum):
+  def forward(ctx, positions, colors, z, batch, L, want_accum, fg_grads=False):
     lib = _lib.load()
     C = colors.shape[1]
     dev = colors.device
@@ -780,6 +782,7 @@ class _Splat(torch.autograd.Function):
     ctx.save_for_forward(positions, colors, z)
     ctx.batch, ctx.L = batch, L
     ctx.want_accum = want_accum
+    ctx.fg_grads = bool(fg_grads) and z is not None
     if want_accum:
       ctx.mark_non_differentiable(accum, norm)
       return out, accum, norm
@@ -811,13 +814,14 @@ class _Splat(torch.autograd.Function):
       d_out = d_out.clone()
     d_colors = torch.empty_like(colors)
     d_pos = torch.empty_like(positions)
+    flags = _lib.DR_SPLAT_FOREGROUND_GRADIENTS if ctx.fg_grads else 0
     with _op("splat_bwd", _splat_launches(ctx.batch, z is not None)):
-      rc = lib.dr_splat_bwd(_p(d_out), _p(positions), _p(z), _p(colors), _p(saved),
-                            colors.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L,
-                            _p(d_colors), _p(d_pos), _stream(d_out.device))
-    _lib.check(rc, "dr_splat_bwd")
+      rc = lib.dr_splat_bwd_ex(_p(d_out), _p(positions), _p(z), _p(colors), _p(saved),
+                               colors.shape[1], ctx.batch.ptr, ctx.batch.n, ctx.L, flags,
+                               _p(d_colors), _p(d_pos), _stream(d_out.device))
+    _lib.check(rc, "dr_splat_bwd_ex")
     return (d_pos if ctx.needs_input_grad[0] else None,
-            d_colors if ctx.needs_input_grad[1] else None, None, None, None, None)
+            d_colors if ctx.needs_input_grad[1] else None, None, None, None, None, None)
 
 
 def split_channels(t, widths, dim=-1):
@@ -841,7 +845,8 @@ def _splat_launches(batch, listed):
   return _groups(batch)
 
 
-def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False, z=None):
+def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=False, z=None,
+                 foreground_gradients=False):
   """Splatted, normalized, composited images [P, C] of a packed batch.
 
   positions [L*P, 4] (viewport xyz, fg) and colors [L*P, C]. ``z`` [L*P],
@@ -849,7 +854,9 @@ def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=Fals
   positions are then not read (nor their position gradients written). With
   ``return_accum_buffers`` also returns the accumulated and normalized
   fg/surface/bg layers, packed [3, H_i, W_i, C] per image (not
-  differentiable).
+  differentiable). ``foreground_gradients`` (with ``z``): the color
+  gradient of background samples is left unwritten, for colors whose VJP
+  reads foreground samples only (the rasterizer's fused interpolation).
   """
   colors = colors.contiguous()
   if colors.dtype != torch.float32:
@@ -862,7 +869,8 @@ def splat_packed(positions, colors, batch, num_layers, return_accum_buffers=Fals
   positions = positions.contiguous()
   if z is not None:
     z = z.detach().contiguous()
-  return _Splat.apply(positions, colors, z, batch, num_layers, bool(return_accum_buffers))
+  return _Splat.apply(positions, colors, z, batch, num_layers, bool(return_accum_buffers),
+                      bool(foreground_gradients))
 
 
 class _Over(torch.autograd.Function):

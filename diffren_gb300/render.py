@@ -55,18 +55,27 @@ def _render_fused(geom, attributes, shading_function, num_layers, face_culling_m
     return None
   cat = torch.cat(parts, dim=1) if len(parts) > 1 else parts[0].contiguous()
   # Background samples are told by the depth buffer downstream, so their
-  # ids and barycentrics need not be written.
+  # ids and barycentrics need not be written; with a pass-through shader
+  # (None) the splat is the only reader of the attributes, so neither are
+  # their attributes nor their color gradients.
+  passthrough = shading_function is None
   cfg = kernels.raster_config(num_layers, face_culling_mode, int(depth_semantics),
-                              flags=kernels._lib.DR_RASTER_FOREGROUND_ONLY)
+                              flags=kernels._lib.DR_RASTER_FOREGROUND_ONLY |
+                              (kernels._lib.DR_RASTER_FOREGROUND_ATTRIBUTES if passthrough
+                               else 0))
   interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
       cat, geom.clip, geom.triangles_packed, geom.batch, cfg,
       kernels.default_workspace(geom.clip.device), recompute_raster)
   frame = rasterize.framebuffer_of(geom, num_layers, ids, z, bary)
   lead = (geom.B,) if geom.batched else ()
   interp = interp.view(*lead, num_layers, frame.height, frame.width, -1)
-  interpolated = dict(zip(keys, kernels.split_channels(interp, widths)))
-  shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
-  return splat.splat_positions(vp, frame, shaded, return_accum_buffers)
+  if passthrough:
+    shaded = interp
+  else:
+    interpolated = dict(zip(keys, kernels.split_channels(interp, widths)))
+    shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
+  return splat.splat_positions(vp, frame, shaded, return_accum_buffers,
+                               foreground_gradients=passthrough)
 
 
 def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
@@ -85,7 +94,10 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   leading batch dimension when the inputs are batched. ``recompute_raster``
   (SPLAT_OVER, beyond the reference's arguments): the backward reruns the
   rasterizer instead of keeping its per-sample triangle ids, barycentrics
-  and vertex ids, for memory-tight renders.
+  and vertex ids, for memory-tight renders. ``shading_function`` None (also
+  beyond the reference's arguments): the single attribute is the color, as
+  ``lambda a: a[key]`` gives, and background samples' attributes and color
+  gradients, which nothing then reads, are not written.
 
   Raises:
     ValueError: if face_culling_mode is not BACK and compositing_mode is
@@ -94,6 +106,8 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   if (compositing_mode == constants.CompositingMode.SPLAT_OVER and
       face_culling_mode != constants.FaceCullingMode.BACK):
     raise ValueError("Backface culling must be enabled when using splatting.")
+  if shading_function is None and len(attributes) != 1:
+    raise ValueError("shading_function=None needs exactly one attribute")
   vertices = torch.as_tensor(vertices)
   triangles = torch.as_tensor(triangles)
   camera = None if camera_matrices is None else torch.as_tensor(camera_matrices)
@@ -110,7 +124,10 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   frame, _ = rasterize.rasterize_geometry(geom, num_layers, face_culling_mode,
                                           depth_semantics, compute_diff_barys)
   interpolated = interpolate.interpolate_vertex_attributes(attributes, frame)
-  shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
+  if shading_function is None:
+    shaded = next(iter(interpolated.values()))
+  else:
+    shaded = _shade_layers(shading_function, interpolated, num_layers, geom.batched)
 
   if compositing_mode == constants.CompositingMode.SPLAT_OVER:
     return splat.splat_clip(geom.clip, frame, shaded, return_accum_buffers)

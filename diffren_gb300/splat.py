@@ -58,13 +58,15 @@ def splat_clip(clip, frame: fb.Framebuffer, shaded_pixels, return_accum_buffers=
 
 
 def splat_positions(positions, frame: fb.Framebuffer, shaded_pixels,
-                    return_accum_buffers=False):
+                    return_accum_buffers=False, foreground_gradients=False):
   """Splat at packed splat positions [L*P, 4] of the framebuffer's samples
-  (background samples are taken from its depth buffer)."""
+  (background samples are taken from its depth buffer).
+  ``foreground_gradients``: see kernels.splat_packed."""
   batch, _, _, z, _ = frame.kernel_inputs()
   colors = _shaded_flat(shaded_pixels)
   res = kernels.splat_packed(positions, colors, batch, frame.num_layers,
-                             return_accum_buffers, z=z)
+                             return_accum_buffers, z=z,
+                             foreground_gradients=foreground_gradients)
   lead = (frame.batch_size,) if frame.is_batched else ()
   return _shape_outputs(res, lead, frame.height, frame.width, colors.shape[1],
                         return_accum_buffers)

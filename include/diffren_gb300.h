@@ -112,6 +112,12 @@ typedef struct dr_raster_config {
  * samples by the depth buffer, as the splat path does; saves 16 bytes per
  * background layer sample. */
 #define DR_RASTER_FOREGROUND_ONLY 1u
+/* dr_raster_config.flags, dr_rasterize_batch_interpolate only: background
+ * samples' interpolated attributes are left unwritten too. For callers whose
+ * only reader of the attributes is the splat given the depth buffer (it
+ * reads colors of foreground samples only); saves 4 K bytes per background
+ * layer sample. */
+#define DR_RASTER_FOREGROUND_ATTRIBUTES 2u
 
 #define DR_MAX_LAYERS 16
 #define DR_MAX_CHANNELS 16
@@ -418,6 +424,17 @@ int dr_splat_bwd(const float* d_out, const float* positions, const float* z_buff
                  const float* colors, const float* saved, int32_t num_channels,
                  const dr_image_desc* images, int32_t num_images, int32_t num_layers,
                  float* d_colors, float* d_positions, void* stream);
+
+/* dr_splat_bwd with flags. DR_SPLAT_FOREGROUND_GRADIENTS (needs z_buffer):
+ * d_colors of background samples are left unwritten as well, for callers
+ * that read the color gradient at foreground samples only (the rasterizer's
+ * fused interpolation VJP does); saves 4 C bytes per background layer
+ * sample. flags = 0 is dr_splat_bwd. */
+#define DR_SPLAT_FOREGROUND_GRADIENTS 1u
+int dr_splat_bwd_ex(const float* d_out, const float* positions, const float* z_buffer,
+                    const float* colors, const float* saved, int32_t num_channels,
+                    const dr_image_desc* images, int32_t num_images, int32_t num_layers,
+                    uint32_t flags, float* d_colors, float* d_positions, void* stream);
 
 /* Forward-mode derivative of dr_splat_fwd's image for tangents of the
  * positions (d_positions [L, H, W, 4], x and y read) and, when non-null, of

@@ -45,7 +45,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_error_string():
   lib = _lib.load()
-  assert lib.dr_abi_version() == 2
+  assert lib.dr_abi_version() == 3
   assert isinstance(lib.dr_last_error(), bytes)
 
 
@@ -54,7 +54,8 @@ def test_workspace_query_rejects_bad_config():
   b = kernels.ImageBatch.single(8, 8, 3, 1)
   for cfg in (kernels.raster_config(0, 0, 0), kernels.raster_config(17, 0, 0),
               kernels.raster_config(1, 5, 0), kernels.raster_config(1, 0, 2),
-              kernels.raster_config(1, 0, 0, tile=(256, 8))):
+              kernels.raster_config(1, 0, 0, tile=(256, 8)),
+              kernels.raster_config(1, 0, 0, flags=4)):
     assert lib.dr_rasterize_batch_workspace_bytes(b.ptr, 1, ctypes.byref(cfg)) == 0
     assert lib.dr_last_error()
   good = kernels.raster_config(3, 1, 0)
@@ -95,6 +96,13 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
   # The backward needs the forward's saved accumulators.
   assert lib.dr_splat_bwd(None, None, None, None, None, 4, b.ptr, 1, 3, None, None,
                           None) == 1
+  # Unknown splat flags; foreground-only color gradients need the depth buffer.
+  saved = ctypes.c_void_p(256)
+  assert lib.dr_splat_bwd_ex(None, None, None, None, saved, 4, b.ptr, 1, 3, 2, None, None,
+                             None) == 1
+  assert lib.dr_splat_bwd_ex(None, None, None, None, saved, 4, b.ptr, 1, 3,
+                             _lib.DR_SPLAT_FOREGROUND_GRADIENTS, None, None, None) == 1
+  assert b"depth buffer" in lib.dr_last_error()
   assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
                                 None) == 1
   assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1

@@ -299,3 +299,110 @@ def test_foreground_only_flag_writes_the_same_foreground(device):
   assert torch.equal(i0[fg], i1[fg]) and torch.equal(b0[fg], b1[fg])
   assert torch.equal(p0[fg], p1[fg])
   assert (a1[~fg] == 0).all()
+
+
+@pytest.mark.parametrize("recompute", [False, True])
+def test_passthrough_shader_gives_the_same_image_and_gradients(recompute, device):
+  """shading_function=None, under which background samples' attributes and
+  color gradients are not written, renders what lambda a: a["rgba"] renders
+  and gives the same gradients (the gradient atomics may reorder float sums:
+  within 1e-6 of the largest magnitude), through BatchRenderer and
+  render_triangles."""
+  meshes, cams, sizes = workloads.ragged_batch(5, seed=13, median_triangles=3000,
+                                               resolutions=(64, 96, 128))
+  r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                              sizes, num_layers=3, device=device, recompute_raster=recompute)
+  cam = torch.tensor(np.stack(cams), device=device)
+  rng = np.random.default_rng(1)
+
+  def grads(out, leaves):
+    g = torch.tensor(rng.standard_normal(tuple(out.shape)).astype(np.float32), device=device)
+    return torch.autograd.grad(out, leaves, g)
+
+  def batched(shader):
+    v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device,
+                     requires_grad=True)
+    c = rgba(torch.tensor(np.concatenate([m.colors for m in meshes]), device=device))
+    c = c.detach().requires_grad_(True)
+    out = r.render(v, {"rgba": c}, cam, shader)
+    return (out.detach(),) + grads(out, (v, c))
+
+  def single(shader):
+    m, cm, (w, h) = meshes[1], cams[1], sizes[1]
+    v = torch.tensor(m.vertices, device=device, requires_grad=True)
+    c = rgba(torch.tensor(m.colors, device=device)).detach().requires_grad_(True)
+    out = render.render_triangles(v, {"rgba": c}, torch.tensor(m.triangles, device=device),
+                                  torch.tensor(cm, device=device), w, h, shader, num_layers=3,
+                                  recompute_raster=recompute)
+    return (out.detach(),) + grads(out, (v, c))
+
+  for run in (batched, single):
+    rng = np.random.default_rng(1)
+    o0, gv0, gc0 = run(rgba_shader)
+    rng = np.random.default_rng(1)
+    o1, gv1, gc1 = run(None)
+    assert torch.equal(o0, o1)
+    for a, b in ((gv0, gv1), (gc0, gc1)):
+      assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
+  with pytest.raises(ValueError):
+    r.render(torch.zeros(r.batch.total_vertices, 3, device=device),
+             {"a": torch.zeros(r.batch.total_vertices, 2, device=device),
+              "b": torch.zeros(r.batch.total_vertices, 2, device=device)}, cam, None)
+
+
+def test_foreground_flags_leave_background_rows_untouched(device):
+  """DR_RASTER_FOREGROUND_ATTRIBUTES and DR_SPLAT_FOREGROUND_GRADIENTS
+  (through the C ABI, into buffers prefilled with NaN): background rows keep
+  their contents, foreground rows are the same bits as without the flags."""
+  meshes, cams, sizes = workloads.ragged_batch(6, seed=17, median_triangles=4000,
+                                               resolutions=(64, 128, 160))
+  from oracle import raster
+  lib = _lib.load()
+  clips = [raster.transform(c, m.vertices) for m, c in zip(meshes, cams)]
+  batch = kernels.ImageBatch([s[0] for s in sizes], [s[1] for s in sizes],
+                             [len(c) for c in clips], [len(m.triangles) for m in meshes])
+  v = torch.as_tensor(np.concatenate(clips), device=device)
+  t = torch.as_tensor(np.concatenate([m.triangles for m in meshes]), device=device)
+  attrs = torch.rand(v.shape[0], 4, device=device)
+  n = 3 * batch.total_pixels
+  P = lambda x: ctypes.c_void_p(x.data_ptr())
+  stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+  outs = []
+  for flags in (_lib.DR_RASTER_FOREGROUND_ONLY,
+                _lib.DR_RASTER_FOREGROUND_ONLY | _lib.DR_RASTER_FOREGROUND_ATTRIBUTES):
+    cfg = kernels.raster_config(3, 1, 0, flags=flags)
+    ws = torch.empty(kernels.raster_workspace_bytes(batch, cfg), dtype=torch.uint8,
+                     device=device)
+    ids = torch.empty(n, dtype=torch.int32, device=device)
+    z = torch.empty(n, device=device)
+    bary = torch.empty(n, 3, device=device)
+    out = torch.full((n, 4), float("nan"), device=device)
+    vp = torch.empty(n, 4, device=device)
+    rc = lib.dr_rasterize_batch_interpolate(P(v), P(t), batch.ptr, batch.n, ctypes.byref(cfg),
+                                            P(ids), P(z), P(bary), P(attrs), 4, P(out), P(vp),
+                                            None, P(ws), ws.numel(), stream)
+    assert rc == 0, lib.dr_last_error()
+    outs.append((z, out, vp))
+  (z0, a0, p0), (z1, a1, p1) = outs
+  fg = z0 != 1.0
+  assert torch.equal(z0, z1) and torch.equal(a0[fg], a1[fg]) and torch.equal(p0[fg], p1[fg])
+  assert (a0[~fg] == 0).all() and torch.isnan(a1[~fg]).all()
+  # Splat forward, then the backward with and without the flag.
+  C = 4
+  img = torch.empty(batch.total_pixels, C, device=device)
+  saved = torch.empty(3 * (C + 1) + 2, batch.total_pixels, device=device)
+  rc = lib.dr_splat_fwd(P(p0), P(z0), P(a0), C, batch.ptr, batch.n, 3, P(img), P(saved), None,
+                        None, stream)
+  assert rc == 0, lib.dr_last_error()
+  d_out = torch.rand(batch.total_pixels, C, device=device) - 0.5
+  res = []
+  for flags in (0, _lib.DR_SPLAT_FOREGROUND_GRADIENTS):
+    d_col = torch.full((n, C), float("nan"), device=device)
+    d_pos = torch.full((n, 4), float("nan"), device=device)
+    rc = lib.dr_splat_bwd_ex(P(d_out), P(p0), P(z0), P(a0), P(saved), C, batch.ptr, batch.n, 3,
+                             flags, P(d_col), P(d_pos), stream)
+    assert rc == 0, lib.dr_last_error()
+    res.append((d_col, d_pos))
+  (c0, q0), (c1, q1) = res
+  assert torch.equal(c0[fg], c1[fg]) and torch.equal(q0[fg], q1[fg])
+  assert (c0[~fg] == 0).all() and torch.isnan(c1[~fg]).all()
