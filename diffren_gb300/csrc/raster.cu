@@ -130,7 +130,10 @@ __device__ __forceinline__ void tile_rect(int4 box, int TW, int TH, int& tx0,
 
 // One thread per triangle of the batch: bounding box, edge matrix, exact
 // coverage cull, per-tile counts (small triangles) or the large list.
-__global__ void __launch_bounds__(256) setup_kernel(RasterArgs a, Batch B) {
+// Bounded to 64 registers so that four blocks share an SM: the kernel waits
+// on its index and vertex loads, and the extra warps hide more of that than
+// the few bytes of spills cost (measured against three blocks and five).
+__global__ void __launch_bounds__(256, 4) setup_kernel(RasterArgs a, Batch B) {
   const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   // Lanes past the end still take part in the warp-wide tile match below.

@@ -209,24 +209,74 @@ __global__ void __launch_bounds__(256) samples_fwd_kernel(SampleArgs a, Batch B)
 
 // Sum of v over lanes lane..last of the calling lane's run (runs are
 // contiguous lanes; `last` is the run's final lane): afterwards each run's
-// first lane holds its total. Every lane of the warp must call it.
+// first lane holds its total. Every lane of the warp must call it. kSteps
+// shuffle steps (d = 1, 2, 4, ...) cover runs of up to 2^kSteps lanes: steps
+// with d above every lane's last - lane add nothing, so a warp whose runs
+// are short takes fewer steps and gets the same bits.
+template <int kSteps>
 __device__ __forceinline__ float run_sum(float v, int lane, int last) {
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
+  for (int k = 0; k < kSteps; ++k) {
+    const int d = 1 << k;
     const float t = __shfl_down_sync(0xffffffffu, v, d);
     if (lane + d <= last) v += t;
   }
   return v;
 }
 
+template <int kSteps>
 __device__ __forceinline__ float4 run_sum4(float4 v, int lane, int last) {
-  return make_float4(run_sum(v.x, lane, last), run_sum(v.y, lane, last),
-                     run_sum(v.z, lane, last), run_sum(v.w, lane, last));
+  return make_float4(run_sum<kSteps>(v.x, lane, last), run_sum<kSteps>(v.y, lane, last),
+                     run_sum<kSteps>(v.z, lane, last), run_sum<kSteps>(v.w, lane, last));
 }
 
 constexpr int kVjpThreads = 512;
 constexpr int kVjpPerThread = 8;  // samples whose depth each thread tests
 constexpr int kVjpBlock = kVjpThreads * kVjpPerThread;
+
+// The run-summed scatter of one compacted foreground sample per lane into
+// the vertex gradients (clip and attributes) and its barycentric adjoint
+// db; kSteps as in run_sum. Every lane of the warp calls it.
+template <int kSteps>
+__device__ __forceinline__ void scatter_runs(const SampleArgs& a, const PosArgs& p,
+                                             const Batch& B, int lane, int last, bool leader,
+                                             bool on, int im, int64_t el, const float (&b)[3],
+                                             const int (&vid)[3], const float4 (&V)[3],
+                                             float4 dcl, float (&db)[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float bi = b[i];
+    float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
+    cv.x = run_sum<kSteps>(cv.x, lane, last);
+    cv.y = run_sum<kSteps>(cv.y, lane, last);
+    cv.w = run_sum<kSteps>(cv.w, lane, last);
+    if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
+      atomicAdd(p.d_clip + B.vertex_offset[im] + vid[i], cv);
+    db[i] = on ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
+  }
+  if (a.d_attr_out) {
+    const int K = a.K;
+    const bool vec_rows = (K & 3) == 0;
+    const float* src = a.d_attr_out + el * K;
+    const int64_t aoff = on ? B.vertex_offset[im] * K : 0;
+    for (int kk = 0; kk < K; kk += 4) {
+      const int nc = min(4, K - kk);
+      const float4 ga = on ? load_chunk(src + kk, nc, vec_rows) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float bi = b[i];
+        float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
+        av = run_sum4<kSteps>(av, lane, last);
+        const int64_t row = aoff + int64_t(vid[i]) * K + kk;
+        if (leader && on) add_chunk(a.d_attr + row, av, nc, vec_rows);
+        if (on && p.d_bary) {
+          const float4 at = load_chunk(a.attr + row, nc, vec_rows);
+          db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
+        }
+      }
+    }
+  }
+}
 
 // VJP of the interpolation and the splat positions. A block takes kVjpBlock
 // consecutive layer samples: each thread tests the depth of kVjpPerThread of
@@ -367,40 +417,19 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
     const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
     const int last = later ? __ffs(later) - 2 : 31;
     const bool leader = ((heads >> lane) & 1u) != 0;
+    // Shuffle steps for the warp's longest run (warp-uniform).
+    const unsigned span = __reduce_max_sync(0xffffffffu, unsigned(last - lane));
     float db[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float bi = b[i];
-      float4 cv = make_float4(bi * dcl.x, bi * dcl.y, 0.0f, bi * dcl.w);
-      cv.x = run_sum(cv.x, lane, last);
-      cv.y = run_sum(cv.y, lane, last);
-      cv.w = run_sum(cv.w, lane, last);
-      if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
-        atomicAdd(p.d_clip + B.vertex_offset[im] + vid[i], cv);
-      db[i] = on ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
-    }
-    if (a.d_attr_out) {
-      const int K = a.K;
-      const bool vec_rows = (K & 3) == 0;
-      const float* src = a.d_attr_out + el * K;
-      const int64_t aoff = on ? B.vertex_offset[im] * K : 0;
-      for (int kk = 0; kk < K; kk += 4) {
-        const int nc = min(4, K - kk);
-        const float4 ga = on ? load_chunk(src + kk, nc, vec_rows) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float bi = b[i];
-          float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
-          av = run_sum4(av, lane, last);
-          const int64_t row = aoff + int64_t(vid[i]) * K + kk;
-          if (leader && on) add_chunk(a.d_attr + row, av, nc, vec_rows);
-          if (on && p.d_bary) {
-            const float4 at = load_chunk(a.attr + row, nc, vec_rows);
-            db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
-          }
-        }
-      }
-    }
+    if (span == 0)
+      scatter_runs<0>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+    else if (span < 2)
+      scatter_runs<1>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+    else if (span < 4)
+      scatter_runs<2>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+    else if (span < 8)
+      scatter_runs<3>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+    else
+      scatter_runs<5>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
     if (on && p.d_bary) {
       p.d_bary[3 * el] = db[0];
       p.d_bary[3 * el + 1] = db[1];

@@ -538,8 +538,12 @@ def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, wa
     d_vp = d_vp.contiguous()
     if d_vp.data_ptr() % 16:
       d_vp = d_vp.clone()
-  d_attr = torch.zeros_like(attributes)
-  d_clip = torch.zeros_like(clip)
+  # Both gradients accumulate (atomics) into one zeroed buffer: one fill.
+  na, nc = attributes.numel(), clip.numel()
+  na_pad = (na + 3) & ~3  # keeps d_clip 16-byte aligned
+  zeros = torch.zeros(na_pad + nc, dtype=torch.float32, device=clip.device)
+  d_attr = zeros[:na].view_as(attributes)
+  d_clip = zeros[na_pad:].view_as(clip)
   d_bary = torch.empty_like(bary) if want_bary else None
   with _op("samples_bwd", _groups(ctx.batch)):
     rc = lib.dr_interpolate_with_positions_bwd(
