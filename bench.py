@@ -140,15 +140,10 @@ LIGHT = (2.0, 2.0, 2.0)
 
 def lit_shader(a):
   """point_light (shaders.py:100-173) with default coefficients on the
-  interpolated RGB, normals and world positions; alpha 1."""
+  interpolated RGB, normals and world positions; alpha 1 (appended by the
+  shader kernel itself on the GPU)."""
   from diffren_gb300 import shaders
-  rgb = shaders.point_light(a["rgb"], a["normals"], a["pos"], LIGHT)
-  return torch_cat_alpha(rgb)
-
-
-def torch_cat_alpha(rgb):
-  import torch
-  return torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+  return shaders.point_light(a["rgb"], a["normals"], a["pos"], LIGHT, alpha=True)
 
 
 def rgba(colors):

@@ -52,6 +52,14 @@ class RasterConfig(ctypes.Structure):
               ("flags", ctypes.c_uint32)]
 
 
+class PointLight(ctypes.Structure):
+  _fields_ = [("light", ctypes.c_float * 3), ("eye", ctypes.c_float * 3),
+              ("ka", ctypes.c_float), ("kd", ctypes.c_float), ("ks", ctypes.c_float),
+              ("ns", ctypes.c_float), ("attenuation_constant", ctypes.c_float),
+              ("attenuation_linear", ctypes.c_float),
+              ("attenuation_quadratic", ctypes.c_float)]
+
+
 SIGNATURES = {
     "dr_last_error": (ctypes.c_char_p, []),
     "dr_abi_version": (_I, []),
@@ -82,6 +90,9 @@ SIGNATURES = {
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_texture_map_fwd": (_I, [_P, _L, _P, _I, _I, _I, _I, _P, _P]),
     "dr_texture_map_bwd": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P]),
+    "dr_point_light_fwd": (_I, [_P, _P, _P, _L, _I, _I, _I, _P, _P, _I, _P]),
+    "dr_point_light_bwd": (_I, [_P, _I, _P, _P, _P, _L, _I, _I, _I, _P, _P, _P, _P, _I,
+                                _P]),
     "dr_composite_over_fwd": (_I, [_P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_composite_over_bwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_squared_error": (_I, [_P, _P, _L, _F, _P, _P, _P, _P]),

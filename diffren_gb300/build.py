@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdiffren_gb300.so")
 SOURCES = ["raster.cu", "interp.cu", "splat.cu", "texture.cu", "normals.cu", "composite.cu",
-           "loss.cu", "abi.cu", "static_scratch.cu"]
+           "loss.cu", "light.cu", "abi.cu", "static_scratch.cu"]
 HEADERS = ["common.cuh", "internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -260,6 +260,31 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                 err);
 }
 
+int dr_point_light_fwd(const float* diffuse, const float* normals, const float* positions,
+                       int64_t num_samples, int32_t diffuse_stride, int32_t normals_stride,
+                       int32_t positions_stride, const dr_point_light* params, float* out,
+                       int32_t out_channels, void* stream) {
+  std::string err;
+  return finish(dr::point_light_fwd_launch(diffuse, normals, positions, num_samples,
+                                           diffuse_stride, normals_stride, positions_stride,
+                                           params, out, out_channels, as_stream(stream), err),
+                err);
+}
+
+int dr_point_light_bwd(const float* d_out, int32_t out_channels, const float* diffuse,
+                       const float* normals, const float* positions, int64_t num_samples,
+                       int32_t diffuse_stride, int32_t normals_stride,
+                       int32_t positions_stride, const dr_point_light* params,
+                       float* d_diffuse, float* d_normals, float* d_positions,
+                       int32_t grad_stride, void* stream) {
+  std::string err;
+  return finish(dr::point_light_bwd_launch(d_out, out_channels, diffuse, normals, positions,
+                                           num_samples, diffuse_stride, normals_stride,
+                                           positions_stride, params, d_diffuse, d_normals,
+                                           d_positions, grad_stride, as_stream(stream), err),
+                err);
+}
+
 int dr_composite_over_fwd(const float* shaded, const float* z_buffer, int32_t channels,
                           const dr_image_desc* images, int32_t num_images, int32_t num_layers,
                           float* out, void* stream) {

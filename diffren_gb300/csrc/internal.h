@@ -108,6 +108,15 @@ int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const flo
                        int H, int W, int C, int flags, float* d_uv, float* d_tex,
                        cudaStream_t stream, std::string& err);
 
+// light.cu
+int point_light_fwd_launch(const float* dif, const float* nrm, const float* pos, int64_t n,
+                           int sd, int sn, int sp, const dr_point_light* q, float* out, int oc,
+                           cudaStream_t stream, std::string& err);
+int point_light_bwd_launch(const float* d_out, int oc, const float* dif, const float* nrm,
+                           const float* pos, int64_t n, int sd, int sn, int sp,
+                           const dr_point_light* q, float* d_dif, float* d_nrm, float* d_pos,
+                           int sg, cudaStream_t stream, std::string& err);
+
 // composite.cu
 int over_fwd_launch(const float* shaded, const float* z, int C, const dr_image_desc* images,
                     int n, int L, float* out, cudaStream_t stream, std::string& err);

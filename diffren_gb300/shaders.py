@@ -4,11 +4,14 @@ diffren/jax/utils/image.py).
 ``texture_map`` is the reference's bilinear texture lookup with edge
 clamping (shaders.py:40-65) and ``bilinear_resample`` the resampler under it
 (image.py:21-118), as one CUDA kernel with a hand-written VJP to the
-coordinates and the image. ``diffuse_light`` and ``point_light``
-(shaders.py:68-173) are the reference's lighting formulas as elementwise
-torch expressions on the interpolated buffers. Any torch function remains
-usable as a shader.
+coordinates and the image. ``diffuse_light``
+(shaders.py:68-97) is the reference's formula as elementwise torch
+expressions; ``point_light`` (shaders.py:100-173) runs as one CUDA kernel
+each way with a hand-written VJP (torch expressions for tensor-valued
+coefficients). Any torch function remains usable as a shader.
 """
+import ctypes
+
 import torch
 
 from . import _lib
@@ -109,13 +112,102 @@ def diffuse_light(diffuse_image, normals_image, light_direction=(0.5, 0.5, 1.0),
   return diffuse_image * ka + diffuse_image * kd * n_dot_l
 
 
+def _row_stride(t):
+  """Row stride (floats) of a [..., 3] float32 tensor whose rows lie evenly
+  spaced in memory (columns of a packed buffer included), else None."""
+  if t.dtype != torch.float32 or t.dim() < 1 or t.shape[-1] != 3 or t.stride(-1) != 1:
+    return None
+  try:
+    rows = t.view(-1, 3)
+  except RuntimeError:
+    return None
+  return 3 if rows.shape[0] <= 1 else rows.stride(0)
+
+
+class _PointLight(torch.autograd.Function):
+  """dr_point_light_fwd / _bwd: the whole shader in one kernel each way."""
+
+  @staticmethod
+  def forward(ctx, diffuse, normals, positions, params, out_channels):
+    lib = _lib.load()
+    ins = []
+    for t in (diffuse, normals, positions):
+      st = _row_stride(t)
+      if st is None or st < 3:
+        t, st = t.float().contiguous(), 3
+      ins.append((t, st))
+    (dif, sd), (nrm, sn), (pos, sp) = ins
+    n = dif.numel() // 3 if dif.dim() > 0 else 0
+    out = torch.empty(n, out_channels, dtype=torch.float32, device=dif.device)
+    with kernels._op("point_light", 1):
+      rc = lib.dr_point_light_fwd(kernels._p(dif), kernels._p(nrm), kernels._p(pos), n, sd, sn,
+                                  sp, ctypes.byref(params), kernels._p(out), out_channels,
+                                  kernels._stream(dif.device))
+    _lib.check(rc, "dr_point_light_fwd")
+    ctx.save_for_backward(dif, nrm, pos)
+    ctx.strides, ctx.params, ctx.oc, ctx.n = (sd, sn, sp), params, out_channels, n
+    ctx.shapes = (diffuse.shape, normals.shape, positions.shape)
+    return out.view(*diffuse.shape[:-1], out_channels)
+
+  @staticmethod
+  def backward(ctx, d_out):
+    dif, nrm, pos = ctx.saved_tensors
+    lib = _lib.load()
+    need = ctx.needs_input_grad[:3]
+    if not any(need):
+      return None, None, None, None, None
+    d_out = d_out.float().contiguous()
+    grads = [torch.empty(ctx.n, 3, dtype=torch.float32, device=dif.device) if w else None
+             for w in need]
+    sd, sn, sp = ctx.strides
+    with kernels._op("point_light_bwd", 1):
+      rc = lib.dr_point_light_bwd(kernels._p(d_out), ctx.oc, kernels._p(dif), kernels._p(nrm),
+                                  kernels._p(pos), ctx.n, sd, sn, sp, ctypes.byref(ctx.params),
+                                  *[kernels._p(g) for g in grads], 3,
+                                  kernels._stream(dif.device))
+    _lib.check(rc, "dr_point_light_bwd")
+    return tuple(None if g is None else g.view(sh) for g, sh in zip(grads, ctx.shapes)) + (
+        None, None)
+
+
+def _three_numbers(v):
+  """v as three Python floats when it is a length-3 sequence of numbers (or
+  a CPU tensor), else None (tensors on the GPU stay on the torch path)."""
+  if torch.is_tensor(v):
+    if v.is_cuda or v.requires_grad or v.numel() != 3:
+      return None
+    return [float(x) for x in v.reshape(-1).tolist()]
+  try:
+    vals = [float(x) for x in v]
+  except (TypeError, ValueError):
+    return None
+  return vals if len(vals) == 3 else None
+
+
 def point_light(diffuse_image, normals_image, pixel_positions, point_locations,
                 eye_position=(0.0, 0.0, 0.0), ka=0.3, kd=1.4, ks=0.0, ns=0.0,
                 attenuation_constant=1.0, attenuation_linear=0.7,
-                attenuation_quadratic=1.8):
+                attenuation_quadratic=1.8, alpha=False):
   """shaders.point_light (shaders.py:100-173): a point light with ambient,
   diffuse and Blinn-Phong specular terms and quadratic distance attenuation
-  1 / (c + l d + q d^2); images are [..., 3]."""
+  1 / (c + l d + q d^2); images are [..., 3]. ``alpha`` (beyond the
+  reference's arguments) appends an alpha channel of 1 (no gradient).
+
+  CUDA images with scalar coefficients and a fixed light and eye run as one
+  kernel each way (dr_point_light_fwd / _bwd); anything else as torch
+  expressions."""
+  light3, eye3 = _three_numbers(point_locations), _three_numbers(eye_position)
+  coefs = (ka, kd, ks, ns, attenuation_constant, attenuation_linear, attenuation_quadratic)
+  tensors = (diffuse_image, normals_image, pixel_positions)
+  if (light3 is not None and eye3 is not None and
+      all(isinstance(c, (int, float)) for c in coefs) and
+      all(torch.is_tensor(t) and t.is_cuda and t.dtype == torch.float32 and t.shape[-1] == 3
+          for t in tensors) and
+      diffuse_image.shape == normals_image.shape == pixel_positions.shape):
+    params = _lib.PointLight((ctypes.c_float * 3)(*light3), (ctypes.c_float * 3)(*eye3),
+                             *[float(c) for c in coefs])
+    return _PointLight.apply(diffuse_image, normals_image, pixel_positions, params,
+                             4 if alpha else 3)
   light = _vec3(point_locations, pixel_positions)
   eye = _vec3(eye_position, pixel_positions)
   to_light = light - pixel_positions
@@ -128,4 +220,7 @@ def point_light(diffuse_image, normals_image, pixel_positions, point_locations,
   decay = 1.0 / (attenuation_constant + attenuation_linear * dist +
                  attenuation_quadratic * dist * dist)
   luma = ka + kd * nol + ks * noh ** ns
-  return diffuse_image * luma * decay
+  rgb = diffuse_image * luma * decay
+  if alpha:
+    rgb = torch.cat([rgb, torch.ones_like(rgb[..., :1])], -1)
+  return rgb

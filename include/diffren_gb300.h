@@ -351,6 +351,34 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                        int32_t channels, int32_t flags, float* d_uv, float* d_texture,
                        void* stream);
 
+/* shaders.point_light (shaders.py:100-173): ambient + diffuse + Blinn-Phong
+ * specular lighting with quadratic distance attenuation, per sample. */
+typedef struct {
+  float light[3];  /* point light location */
+  float eye[3];    /* eye location */
+  float ka, kd, ks, ns;
+  float attenuation_constant, attenuation_linear, attenuation_quadratic;
+} dr_point_light;
+
+/* diffuse, normals and positions are rows of 3 floats, `*_stride` floats
+ * apart (>= 3; columns of one packed attribute buffer can be passed in
+ * place); out [num_samples, out_channels], out_channels 3, or 4 with the
+ * last channel (alpha) set to 1. */
+int dr_point_light_fwd(const float* diffuse, const float* normals, const float* positions,
+                       int64_t num_samples, int32_t diffuse_stride, int32_t normals_stride,
+                       int32_t positions_stride, const dr_point_light* params, float* out,
+                       int32_t out_channels, void* stream);
+
+/* Its VJP for d_out [num_samples, out_channels] (the alpha gradient is
+ * ignored): d_diffuse, d_normals and d_positions (each nullable) are
+ * written as rows `grad_stride` floats apart. */
+int dr_point_light_bwd(const float* d_out, int32_t out_channels, const float* diffuse,
+                       const float* normals, const float* positions, int64_t num_samples,
+                       int32_t diffuse_stride, int32_t normals_stride,
+                       int32_t positions_stride, const dr_point_light* params,
+                       float* d_diffuse, float* d_normals, float* d_positions,
+                       int32_t grad_stride, void* stream);
+
 /* ------------------------------------------------------ compositing */
 
 /* CompositingMode.OVER of render_triangles (render.py:134-140): shaded

@@ -42,3 +42,20 @@ def test_l2_normalize_matches_reference_formula():
   x = torch.tensor([[3.0, 4.0, 0.0], [0.0, 0.0, 0.0]])
   np.testing.assert_allclose(shaders.l2_normalize(x).numpy(), [[0.6, 0.8, 0.0], [0, 0, 0]],
                              rtol=1e-6)
+
+
+def test_point_light_row_strides_and_alpha_on_cpu():
+  """The fused kernel reads rows evenly spaced in memory (columns of one
+  packed buffer); CPU tensors take the torch expressions, and ``alpha``
+  appends an alpha of 1 there too."""
+  buf = torch.zeros(10, 9)
+  assert shaders._row_stride(buf[:, 3:6]) == 9
+  assert shaders._row_stride(buf[:, 6:9].view(1, -1, 3)) == 9
+  assert shaders._row_stride(torch.zeros(4, 5, 3)) == 3
+  assert shaders._row_stride(torch.zeros(3, 4, 3).transpose(0, 1)) is None
+  assert shaders._row_stride(torch.zeros(4, 3, dtype=torch.float64)) is None
+  rng = np.random.default_rng(4)
+  c, n, p = (torch.tensor(rng.uniform(-1, 1, (6, 3)), dtype=torch.float32) for _ in range(3))
+  rgb = shaders.point_light(c, n, p, (2.0, 1.0, 2.0))
+  rgba = shaders.point_light(c, n, p, (2.0, 1.0, 2.0), alpha=True)
+  assert rgba.shape == (6, 4) and torch.equal(rgba[:, :3], rgb) and (rgba[:, 3] == 1).all()
