@@ -5,10 +5,8 @@ icospheres or triangle soups, 50/50), triangle counts lognormal (median 20k,
 sigma 1.2) clipped to [500, 500k], one camera per mesh on a sphere of radius
 3, square resolutions drawn from {256, 512, 1024}, 3 depth layers, back-face
 culling, RGBA vertex colors (RGB seeded, alpha 1) interpolated as an
-attribute and used as the splat colors (shading_function=None, the
-pass-through `lambda a: a['rgba']` of the reference's render tests, under
-which background samples' attributes and color gradients are not written;
-both arms render this way). One step = forward
+attribute and passed through by the deferred shader (`lambda a: a['rgba']`,
+as the reference's render tests shade). One step = forward
 render of every image + L2 loss against fixed target images + backward to
 vertex positions and vertex colors (the optimized color parameter is the
 RGBA vertex color; the RGB gradients are its first three columns).
@@ -130,9 +128,10 @@ class Workload:
       t[..., 3] = 1.0
 
 
-# Pass-through of the interpolated RGBA vertex colors (the reference's
-# render tests shade with `lambda x: x['rgba']`): the renderers' None.
-shader = None
+def shader(a):
+  """Pass-through of the interpolated RGBA vertex colors (the reference's
+  render tests shade with `lambda x: x['rgba']` the same way)."""
+  return a["rgba"]
 
 
 LIGHT = (2.0, 2.0, 2.0)
@@ -271,27 +270,29 @@ TRAFFIC_PER_SAMPLE = {"raster": 44.3, "splat_fwd": 24.48, "splat_bwd": 43.46,
                       "samples_bwd": 23.15}
 
 
-def kernel_bytes(wl, fg, near=None, C=4, K=4, passthrough=False, vids=True):
+def kernel_bytes(wl, fg, near=None, C=4, K=4, fg_attributes=False, fg_color_grads=False,
+                 vids=True):
   """Algorithmic (compulsory) HBM bytes per launch of each kernel: every
   input read and every output written once. `fg` = foreground layer samples
   among the L * P; work on background samples stops after their depth.
   `near` = pixels within one pixel of a foreground sample (the only ones
   whose splat accumulators the backward needs); all pixels if None.
-  `passthrough`: the splat colors are the interpolated attributes
-  (shading_function None), so background attributes and color gradients
-  are not written. `vids`: the rasterizer stores vertex ids (no
-  recompute)."""
+  `fg_attributes`: background attributes are not written (shading_function
+  None); `fg_color_grads`: nor background color gradients (the splat colors
+  are the interpolated attributes). `vids`: the rasterizer stores vertex ids
+  (no recompute)."""
   L, P, T, V = wl.num_layers, wl.pixels, wl.triangles, wl.vertices
   S = L * P
   near = P if near is None else near
-  written = fg if passthrough else S  # samples whose attributes / d colors are written
+  attr_written = fg if fg_attributes else S  # samples whose attributes are written
+  grad_written = fg if fg_color_grads else S  # samples whose d colors are written
   return {
       # rasterizer with the fused interpolation epilogue: the mesh (indices,
       # clip vertices, attributes) in; z of every sample, ids, barycentrics,
       # viewport position (and vertex ids) of every foreground sample and K
       # attributes of the written samples out
       "raster": (T * 12 + V * (16 + 4 * K) + 4 * S + fg * (16 + 16 + (12 if vids else 0))
-                 + 4 * K * written),
+                 + 4 * K * attr_written),
       # depth of every sample, position and color of every foreground
       # sample in; composited color per pixel, saved accumulators (3 (C + 1))
       # and the surface code per pixel near foreground out
@@ -301,7 +302,7 @@ def kernel_bytes(wl, fg, near=None, C=4, K=4, passthrough=False, vids=True):
       # foreground ones in; d color of the written samples and d position of
       # every foreground sample out
       "splat_bwd": (near * (12 * (C + 1) + 4 + 4 * C) + 4 * S + (16 + 4 * C) * fg
-                    + 4 * C * written + 16 * fg),
+                    + 4 * C * grad_written + 16 * fg),
       # z of every sample; ids, bary, d position and d attributes of the
       # depth of every sample; barycentrics, vertex indices, d position,
       # position and d attributes of the foreground ones; vertex gradients
@@ -794,7 +795,7 @@ def main():
   peak, peak_kind = measured_peaks()
   pk = res["per_kernel"]
   nbytes = kernel_bytes(wl, res["fg"], res["near"], K=2 if wl.texture is not None else 4,
-                        passthrough=wl.texture is None and not wl.lit,
+                        fg_color_grads=wl.texture is None and not wl.lit,
                         vids=not args.recompute_raster)
   dom = max((k for k in pk if k in nbytes), key=lambda k: pk[k])
   achieved = nbytes[dom] / (pk[dom] * 1e-3) / 1e9

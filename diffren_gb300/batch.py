@@ -156,8 +156,15 @@ class BatchRenderer:
       shaded = shading_function({k: s.view(1, -1, s.shape[1]) for k, s in zip(keys, split)})
       shaded = shaded.reshape(-1, shaded.shape[-1])
     if splatting:
+      # Colors that are the fused pass's attribute buffer itself (a
+      # pass-through shader such as lambda a: a[key]) send their gradient
+      # only to that pass's VJP, which reads foreground samples: background
+      # color gradients need not be written.
+      colors_are_attributes = fused and (passthrough or (
+          shaded.data_ptr() == interp.data_ptr() and shaded.shape == interp.shape and
+          shaded.stride() == interp.stride()))
       return kernels.splat_packed(vp, shaded, b, L, return_accum_buffers, z=z,
-                                  foreground_gradients=passthrough and fused)
+                                  foreground_gradients=colors_are_attributes)
     if compositing_mode == constants.CompositingMode.NONE:
       return shaded * (z != 1.0).float()[:, None]
     return kernels.over_packed(shaded, z, b, L)

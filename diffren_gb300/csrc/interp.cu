@@ -20,39 +20,106 @@ __device__ __forceinline__ int3 load_tri(const int32_t* tris, const Batch& B, in
 }
 
 // -------------------------------------------------------------- transform
-__global__ void transform_kernel(const float* __restrict__ M, const float* __restrict__ v,
-                                 int dim, Batch B, float4* __restrict__ out) {
-  const int64_t total = B.pix_prefix[B.n];  // total vertices (reused field)
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  const int img = find_segment(B.pix_prefix, B.n, i);
-  const int64_t vi = B.vertex_offset[img] + (i - B.pix_prefix[img]);
-  const float* m = M + 16 * img;
-  const float x = v[dim * vi], y = v[dim * vi + 1], z = v[dim * vi + 2];
-  const float w = dim == 4 ? v[dim * vi + 3] : 1.0f;
+// Each thread takes kVertsPerThread consecutive vertices: one image lookup,
+// and for xyz vertices of one image starting on a 16-byte boundary three
+// 16-byte loads (or stores, backward) cover the four rows.
+constexpr int kVertsPerThread = 4;
+
+// Row r of M times (x, y, z, w), products rounded and summed in order.
+__device__ __forceinline__ float4 transform_one(const float (&m)[16], float x, float y, float z,
+                                                float w) {
   float r[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     r[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4 * k], x), __fmul_rn(m[4 * k + 1], y)),
                                __fmul_rn(m[4 * k + 2], z)),
                      __fmul_rn(m[4 * k + 3], w));
-  out[vi] = make_float4(r[0], r[1], r[2], r[3]);
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// d_v[c] = sum_r d_clip[r] M[r][c], in the order r = 0..3, fused.
+__device__ __forceinline__ float transform_vjp(const float (&m)[16], float4 g, int c) {
+  return __fmaf_rn(g.w, m[12 + c], __fmaf_rn(g.z, m[8 + c], __fmaf_rn(g.y, m[4 + c],
+                                                                     __fmul_rn(g.x, m[c]))));
+}
+
+__device__ __forceinline__ void load_matrix(const float* M, int img, float (&m)[16]) {
+#pragma unroll
+  for (int k = 0; k < 16; ++k) m[k] = __ldg(M + 16 * img + k);
+}
+
+// The image holding dense vertex i (at or after `img`) and its packed index.
+__device__ __forceinline__ int64_t packed_vertex(const Batch& B, int64_t i, int& img) {
+  while (img + 1 < B.n && i >= B.pix_prefix[img + 1]) ++img;
+  return B.vertex_offset[img] + (i - B.pix_prefix[img]);
+}
+
+// `vec`: v (dim 3) and out are 16-byte aligned.
+__global__ void transform_kernel(const float* __restrict__ M, const float* __restrict__ v,
+                                 int dim, Batch B, float4* __restrict__ out, bool vec) {
+  const int64_t total = B.pix_prefix[B.n];  // total vertices (reused field)
+  const int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kVertsPerThread;
+  if (i0 >= total) return;
+  int img = find_segment(B.pix_prefix, B.n, i0);
+  float m[16];
+  load_matrix(M, img, m);
+  const int64_t vi0 = B.vertex_offset[img] + (i0 - B.pix_prefix[img]);
+  if (vec && dim == 3 && i0 + kVertsPerThread <= B.pix_prefix[img + 1] && (vi0 & 3) == 0) {
+    const float4* src = reinterpret_cast<const float4*>(v + 3 * vi0);
+    const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+    out[vi0] = transform_one(m, a.x, a.y, a.z, 1.0f);
+    out[vi0 + 1] = transform_one(m, a.w, b.x, b.y, 1.0f);
+    out[vi0 + 2] = transform_one(m, b.z, b.w, c.x, 1.0f);
+    out[vi0 + 3] = transform_one(m, c.y, c.z, c.w, 1.0f);
+    return;
+  }
+  const int img0 = img;
+  for (int u = 0; u < kVertsPerThread; ++u) {
+    const int64_t i = i0 + u;
+    if (i >= total) break;
+    const int64_t vi = packed_vertex(B, i, img);
+    if (img != img0) load_matrix(M, img, m);
+    const float* p = v + dim * vi;
+    const float w = dim == 4 ? __ldg(p + 3) : 1.0f;
+    out[vi] = transform_one(m, __ldg(p), __ldg(p + 1), __ldg(p + 2), w);
+  }
 }
 
 // VJP of transform_kernel w.r.t. the vertices: d_v[c] = sum_r d_clip[r] M[r][c]
-// for c < dim.
+// for c < dim. `vec`: d_v (dim 3) is 16-byte aligned.
 __global__ void transform_bwd_kernel(const float* __restrict__ M,
                                      const float4* __restrict__ d_clip, int dim, Batch B,
-                                     float* __restrict__ d_v) {
+                                     float* __restrict__ d_v, bool vec) {
   const int64_t total = B.pix_prefix[B.n];
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  const int img = find_segment(B.pix_prefix, B.n, i);
-  const int64_t vi = B.vertex_offset[img] + (i - B.pix_prefix[img]);
-  const float* m = M + 16 * img;
-  const float4 g = d_clip[vi];
-  for (int c = 0; c < dim; ++c)
-    d_v[dim * vi + c] = g.x * m[c] + g.y * m[4 + c] + g.z * m[8 + c] + g.w * m[12 + c];
+  const int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kVertsPerThread;
+  if (i0 >= total) return;
+  int img = find_segment(B.pix_prefix, B.n, i0);
+  float m[16];
+  load_matrix(M, img, m);
+  const int64_t vi0 = B.vertex_offset[img] + (i0 - B.pix_prefix[img]);
+  if (vec && dim == 3 && i0 + kVertsPerThread <= B.pix_prefix[img + 1] && (vi0 & 3) == 0) {
+    float r[12];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float4 g = __ldg(d_clip + vi0 + u);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[3 * u + c] = transform_vjp(m, g, c);
+    }
+    float4* dst = reinterpret_cast<float4*>(d_v + 3 * vi0);
+    dst[0] = make_float4(r[0], r[1], r[2], r[3]);
+    dst[1] = make_float4(r[4], r[5], r[6], r[7]);
+    dst[2] = make_float4(r[8], r[9], r[10], r[11]);
+    return;
+  }
+  const int img0 = img;
+  for (int u = 0; u < kVertsPerThread; ++u) {
+    const int64_t i = i0 + u;
+    if (i >= total) break;
+    const int64_t vi = packed_vertex(B, i, img);
+    if (img != img0) load_matrix(M, img, m);
+    const float4 g = __ldg(d_clip + vi);
+    for (int c = 0; c < dim; ++c) d_v[dim * vi + c] = transform_vjp(m, g, c);
+  }
 }
 
 // ---------------------------------------------------------- interpolation
@@ -323,9 +390,11 @@ int transform_launch(const float* M, const float* v, int dim, const dr_image_des
       acc += images[g0 + i].num_vertices;
     }
     b.pix_prefix[cnt] = acc;
+    const int64_t per_block = 256 * kVertsPerThread;
+    const bool vec = ((reinterpret_cast<uintptr_t>(v) | reinterpret_cast<uintptr_t>(clip)) & 15) == 0;
     if (acc > 0)
-      transform_kernel<<<unsigned((acc + 255) / 256), 256, 0, stream>>>(
-          M + 16 * g0, v, dim, b, reinterpret_cast<float4*>(clip));
+      transform_kernel<<<unsigned((acc + per_block - 1) / per_block), 256, 0, stream>>>(
+          M + 16 * g0, v, dim, b, reinterpret_cast<float4*>(clip), vec);
   }
   return launch_status("transform", err);
 }
@@ -350,9 +419,11 @@ int transform_bwd_launch(const float* M, const float* d_clip, int dim,
       acc += images[g0 + i].num_vertices;
     }
     b.pix_prefix[cnt] = acc;
+    const int64_t per_block = 256 * kVertsPerThread;
+    const bool vec = (reinterpret_cast<uintptr_t>(d_vertices) & 15) == 0;
     if (acc > 0)
-      transform_bwd_kernel<<<unsigned((acc + 255) / 256), 256, 0, stream>>>(
-          M + 16 * g0, reinterpret_cast<const float4*>(d_clip), dim, b, d_vertices);
+      transform_bwd_kernel<<<unsigned((acc + per_block - 1) / per_block), 256, 0, stream>>>(
+          M + 16 * g0, reinterpret_cast<const float4*>(d_clip), dim, b, d_vertices, vec);
   }
   return launch_status("transform backward", err);
 }

@@ -75,7 +75,8 @@ def test_kernel_bytes_formulas():
   assert b["splat_fwd"] == 4 * S + 32 * 400 + 16 * 1000 + 64 * 600
   assert b["splat_bwd"] == 600 * 80 + 4 * S + 32 * 400 + 16 * S + 16 * 400
   # pass-through colors: background attributes and color gradients unwritten
-  p = bench.kernel_bytes(wl, fg=400, near=600, C=4, K=4, passthrough=True, vids=False)
+  p = bench.kernel_bytes(wl, fg=400, near=600, C=4, K=4, fg_attributes=True,
+                         fg_color_grads=True, vids=False)
   assert p["raster"] == 50 * 12 + 30 * 32 + S * 4 + 400 * 32 + 16 * 400
   assert p["splat_bwd"] == 600 * 80 + 4 * S + 32 * 400 + 16 * 400 + 16 * 400
   assert b["samples_bwd"] == 4 * S + 400 * 64 + 30 * 32 * 3
