@@ -262,12 +262,12 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- our arm
 # DRAM bytes (read + write) per layer sample of each op, from the ncu
-# capture of the 8-mesh subset of the ragged workload
-# (profiles/*_ragged8_subset.md): setup + tile scan + binning + fine raster;
+# capture of the 8-mesh subset of the ragged workload (the summaries under
+# profiles/): setup + tile scan + binning + fine raster;
 # splat forward; splat backward; samples VJP. Traffic grows with the layer
 # samples, so the full workload's traffic is this times its samples.
-TRAFFIC_PER_SAMPLE = {"raster": 44.3, "splat_fwd": 24.48, "splat_bwd": 43.46,
-                      "samples_bwd": 23.15}
+TRAFFIC_PER_SAMPLE = {"raster": 32.98, "splat_fwd": 22.61, "splat_bwd": 31.73,
+                      "samples_bwd": 22.92}
 
 
 def kernel_bytes(wl, fg, near=None, C=4, K=4, fg_attributes=False, fg_color_grads=False,
