@@ -64,6 +64,9 @@ def parse():
   ap.add_argument("--recompute-raster", action="store_true",
                   help="the VJP reruns the rasterizer instead of keeping its ids, "
                        "barycentrics and vertex ids (memory-tight mode)")
+  ap.add_argument("--deterministic-gradients", action="store_true",
+                  help="sum the vertex and color gradients in fixed point (same bits on "
+                       "every run)")
   ap.add_argument("--cpu-budget", type=float, default=20.0,
                   help="seconds of CPU work per reference-arm step / baseline")
   return ap.parse_args()
@@ -343,7 +346,8 @@ def run_ours(args, rank, world, device):
   r = batch_lib.BatchRenderer([m.triangles for m in wl.meshes],
                               [len(m.vertices) for m in wl.meshes], wl.sizes,
                               num_layers=wl.num_layers, device=device, tile="auto",
-                              recompute_raster=args.recompute_raster)
+                              recompute_raster=args.recompute_raster,
+                              deterministic_gradients=args.deterministic_gradients)
   from diffren_gb300 import shaders
   textured = wl.texture is not None
   verts_h = torch.from_numpy(np.concatenate([m.vertices for m in wl.meshes])).pin_memory()
@@ -812,6 +816,7 @@ def main():
                   "cuda_graph": True, "raster_tile_autotuned": res["tile"],
                   "depth_semantics": "discretized (the reference CUDA rasterizer's)",
                   "recompute_raster": bool(args.recompute_raster),
+                  "deterministic_gradients": bool(args.deterministic_gradients),
                   "step_peak_device_bytes": res["step_peak_bytes"]},
       "parity": parity,
       "e2e": {"value": whole_job_mpix(world, wl.pixels, res["ms_e2e"]), "unit": "Mpix/s",

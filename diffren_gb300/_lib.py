@@ -18,6 +18,7 @@ DR_FLAG_NONFINITE_VERTEX = 2
 DR_RASTER_FOREGROUND_ONLY = 1
 DR_RASTER_FOREGROUND_ATTRIBUTES = 2
 DR_SPLAT_FOREGROUND_GRADIENTS = 1
+DR_SAMPLES_DETERMINISTIC = 1
 DR_MAX_LAYERS = 16
 DR_MAX_CHANNELS = 16
 DR_MAX_SPLAT_CHANNELS = 8
@@ -86,6 +87,10 @@ SIGNATURES = {
                                               _P, _P, _P]),
     "dr_interpolate_with_positions_bwd": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _P,
                                               _P, _I, _I, _P, _P, _P, _P]),
+    "dr_interpolate_with_positions_bwd_ex": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P,
+                                                 _P, _P, _I, _I, ctypes.c_uint32, _P, _P,
+                                                 _P, _P, _S, _P]),
+    "dr_interpolate_with_positions_bwd_scratch_bytes": (_S, [_P, _I, _I]),
     "dr_splat_positions_fwd": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_texture_map_fwd": (_I, [_P, _L, _P, _I, _I, _I, _I, _P, _P]),

@@ -32,13 +32,17 @@ class BatchRenderer:
                resolutions: Sequence, num_layers: int = 1,
                face_culling_mode=constants.FaceCullingMode.BACK,
                depth_semantics=constants.DepthSemantics.CUDA, device=None,
-               tile=(0, 0), large_tiles=0, recompute_raster=False):
+               tile=(0, 0), large_tiles=0, recompute_raster=False,
+               deterministic_gradients=False):
     """``tile`` = (width, height) of the rasterizer's tiles, (0, 0) for the
     default, or "auto" to let the autotuner pick the tile and the
     large-triangle threshold on the first render (see autotune.py).
     ``recompute_raster``: for memory-tight batches, the backward reruns the
     rasterizer instead of keeping the triangle ids, barycentrics and vertex
-    ids of every layer sample from the forward (28 bytes per sample)."""
+    ids of every layer sample from the forward (28 bytes per sample).
+    ``deterministic_gradients``: the vertex and attribute gradients of the
+    fused pass are summed in fixed point instead of with float atomics, so
+    they are the same bits on every run (one more pass over the samples)."""
     if len(triangles) != len(vertex_counts) or len(triangles) != len(resolutions):
       raise ValueError("triangles, vertex_counts and resolutions differ in length")
     self.device = torch.device(device or "cuda")
@@ -59,6 +63,7 @@ class BatchRenderer:
     self.workspace = kernels.Workspace(self.device)
     self.workspace.get(kernels.raster_workspace_bytes(self.batch, self.config))
     self.recompute_raster = bool(recompute_raster)
+    self.deterministic_gradients = bool(deterministic_gradients)
 
   def autotune(self, clip, attributes=None, **kw):
     """Picks the fastest tile / large-triangle configuration for this batch
@@ -141,7 +146,7 @@ class BatchRenderer:
       interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
           cat, clip, self.triangles, b,
           kernels.foreground_only(self.config, attributes=passthrough), self.workspace,
-          self.recompute_raster)
+          self.recompute_raster, self.deterministic_gradients)
     else:
       ids, z, bary = self.rasterize(clip)
       if splatting:

@@ -220,6 +220,24 @@ int dr_interpolate_with_positions_fwd(const float* attributes, int32_t num_chann
                 err);
 }
 
+int dr_interpolate_with_positions_bwd_ex(
+    const float* d_attributes_out, const float* d_positions, const float* attributes,
+    int32_t num_channels, const float* clip_vertices, const int32_t* triangles,
+    const int32_t* triangle_ids, const float* z_buffer, const float* barycentrics,
+    const float* positions, const int32_t* vertex_ids, const dr_image_desc* images,
+    int32_t num_images, int32_t num_layers, uint32_t flags, float* d_attributes,
+    float* d_clip_vertices, float* d_barycentrics, void* scratch, size_t scratch_bytes,
+    void* stream) {
+  std::string err;
+  return finish(dr::samples_bwd_launch(d_attributes_out, d_positions, attributes,
+                                       num_channels, clip_vertices, triangles,
+                                       triangle_ids, z_buffer, barycentrics, positions,
+                                       vertex_ids, images, num_images, num_layers,
+                                       d_attributes, d_clip_vertices, d_barycentrics, flags,
+                                       scratch, scratch_bytes, as_stream(stream), err),
+                err);
+}
+
 int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       const float* d_positions, const float* attributes,
                                       int32_t num_channels, const float* clip_vertices,
@@ -230,14 +248,19 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       int32_t num_layers, float* d_attributes,
                                       float* d_clip_vertices, float* d_barycentrics,
                                       void* stream) {
-  std::string err;
-  return finish(dr::samples_bwd_launch(d_attributes_out, d_positions, attributes,
-                                       num_channels, clip_vertices, triangles,
-                                       triangle_ids, z_buffer, barycentrics, positions,
-                                       vertex_ids, images, num_images, num_layers,
-                                       d_attributes, d_clip_vertices, d_barycentrics,
-                                       as_stream(stream), err),
-                err);
+  return dr_interpolate_with_positions_bwd_ex(
+      d_attributes_out, d_positions, attributes, num_channels, clip_vertices, triangles,
+      triangle_ids, z_buffer, barycentrics, positions, vertex_ids, images, num_images,
+      num_layers, 0u, d_attributes, d_clip_vertices, d_barycentrics, nullptr, 0, stream);
+}
+
+size_t dr_interpolate_with_positions_bwd_scratch_bytes(const dr_image_desc* images,
+                                                       int32_t num_images,
+                                                       int32_t num_channels) {
+  if (num_images < 0 || (num_images > 0 && !images) || num_channels < 1 ||
+      num_channels > DR_MAX_CHANNELS)
+    return 0;
+  return dr::samples_fixed_bytes(images, num_images, num_channels);
 }
 
 int dr_texture_map_fwd(const float* uv, int64_t num_points, const float* texture,

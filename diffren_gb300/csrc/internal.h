@@ -150,7 +150,9 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
                        const float* bary, const float* positions,
                        const int32_t* vertex_ids, const dr_image_desc* images, int n,
                        int L, float* d_attributes, float* d_clip, float* d_bary,
+                       uint32_t flags, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, std::string& err);
+size_t samples_fixed_bytes(const dr_image_desc* images, int n, int K);
 int positions_fwd_launch(const float* clip, const int32_t* tris, const int32_t* ids,
                          const float* z, const float* bary, const dr_image_desc* images,
                          int n, int L, float* positions, cudaStream_t stream,

@@ -158,7 +158,59 @@ struct SampleArgs {
   float* attr_out;         // [L*P, K]
   const float* d_attr_out;  // backward input (nullable)
   float* d_attr;            // [V, K] accumulated
+  // DR_SAMPLES_DETERMINISTIC: the vertex gradients are summed in 64-bit
+  // fixed point, 2^e units per unit with e chosen from the largest value
+  // added, so that the sums do not depend on the order of the atomics.
+  unsigned* fx_max;              // [1] float bits of the largest |value| added
+  unsigned long long* fx_clip;   // [V, 4] fixed-point sums
+  unsigned long long* fx_attr;   // [V, K]
+  int fx_log2_count;             // ceil(log2(bound on the additions per sum))
 };
+
+// Exponent e of the fixed-point sums (2^e units per unit) from the largest
+// magnitude added: every sum of at most 2^log2_count values stays below
+// 2^62. kFixedZero when nothing but zeros is added, kFixedFloat when a value
+// is not finite (those sums fall back to float atomics, which propagate the
+// inf / NaN as the float path does).
+constexpr int kFixedZero = -100000, kFixedFloat = -200000;
+constexpr int kRunBits = 6;  // 32 lanes per run, and margin for rounding
+
+__device__ __forceinline__ int fixed_exponent(const SampleArgs& a) {
+  const float m = __uint_as_float(__ldg(a.fx_max));
+  if (!(m <= 3.402823466e38f)) return kFixedFloat;
+  if (m == 0.0f) return kFixedZero;
+  return 61 - kRunBits - ilogbf(m) - a.fx_log2_count;
+}
+
+// round(v 2^e) in integer arithmetic: v = m 2^x with a 24-bit integer m, so
+// v 2^e = m 2^(x + e), shifted left exactly or right with rounding to
+// nearest, ties to even (|v 2^e| < 2^62 by the choice of e).
+__device__ __forceinline__ long long fixed_of(float v, int e) {
+  const unsigned u = __float_as_uint(v);
+  const int bexp = int((u >> 23) & 0xffu);
+  const unsigned m = bexp ? ((u & 0x7fffffu) | 0x800000u) : (u & 0x7fffffu);
+  const int sh = (bexp ? bexp - 150 : -149) + e;
+  long long r;
+  if (sh >= 0) {
+    r = (long long)m << sh;
+  } else if (sh < -24) {
+    r = 0;  // m 2^sh < 1/2
+  } else {
+    const int s = -sh;
+    const unsigned q = m >> s, rem = m & ((1u << s) - 1u), half = 1u << (s - 1);
+    r = (long long)(q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u));
+  }
+  return (u >> 31) ? -r : r;
+}
+
+__device__ __forceinline__ void add_fixed(unsigned long long* p, float v, int e) {
+  atomicAdd(p, (unsigned long long)fixed_of(v, e));
+}
+
+// |v| for the fixed-point scale, +inf for a non-finite v.
+__device__ __forceinline__ float fixed_mag(float v) {
+  return isfinite(v) ? fabsf(v) : __int_as_float(0x7f800000);
+}
 
 __device__ __forceinline__ void add_chunk(float* p, float4 v, int n, bool vec) {
   if (vec) {
@@ -237,12 +289,17 @@ constexpr int kVjpBlock = kVjpThreads * kVjpPerThread;
 // The run-summed scatter of one compacted foreground sample per lane into
 // the vertex gradients (clip and attributes) and its barycentric adjoint
 // db; kSteps as in run_sum. Every lane of the warp calls it.
-template <int kSteps>
+// kMode 0 adds with float atomics; kMode 2 adds in fixed point at exponent
+// `scale` (float atomics for kFixedFloat; nothing for kFixedZero, as only
+// zeros would be added). The first deterministic pass (kMode 1) does not
+// get here.
+template <int kSteps, int kMode>
 __device__ __forceinline__ void scatter_runs(const SampleArgs& a, const PosArgs& p,
                                              const Batch& B, int lane, int last, bool leader,
                                              bool on, int im, int64_t el, const float (&b)[3],
                                              const int (&vid)[3], const float4 (&V)[3],
-                                             float4 dcl, float (&db)[3]) {
+                                             float4 dcl, float (&db)[3], float& mx,
+                                             int scale) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const float bi = b[i];
@@ -250,8 +307,16 @@ __device__ __forceinline__ void scatter_runs(const SampleArgs& a, const PosArgs&
     cv.x = run_sum<kSteps>(cv.x, lane, last);
     cv.y = run_sum<kSteps>(cv.y, lane, last);
     cv.w = run_sum<kSteps>(cv.w, lane, last);
-    if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f))
+    if (kMode == 2 && scale != kFixedFloat) {
+      if (leader && on && scale != kFixedZero) {
+        unsigned long long* q = a.fx_clip + 4 * (B.vertex_offset[im] + vid[i]);
+        add_fixed(q, cv.x, scale);
+        add_fixed(q + 1, cv.y, scale);
+        add_fixed(q + 3, cv.w, scale);
+      }
+    } else if (leader && on && (cv.x != 0.0f || cv.y != 0.0f || cv.w != 0.0f)) {
       atomicAdd(p.d_clip + B.vertex_offset[im] + vid[i], cv);
+    }
     db[i] = on ? V[i].x * dcl.x + V[i].y * dcl.y + V[i].w * dcl.w : 0.0f;
   }
   if (a.d_attr_out) {
@@ -268,7 +333,14 @@ __device__ __forceinline__ void scatter_runs(const SampleArgs& a, const PosArgs&
         float4 av = make_float4(bi * ga.x, bi * ga.y, bi * ga.z, bi * ga.w);
         av = run_sum4<kSteps>(av, lane, last);
         const int64_t row = aoff + int64_t(vid[i]) * K + kk;
-        if (leader && on) add_chunk(a.d_attr + row, av, nc, vec_rows);
+        if (kMode == 2 && scale != kFixedFloat) {
+          if (leader && on && scale != kFixedZero) {
+            const float vv[4] = {av.x, av.y, av.z, av.w};
+            for (int c = 0; c < nc; ++c) add_fixed(a.fx_attr + row + c, vv[c], scale);
+          }
+        } else if (leader && on) {
+          add_chunk(a.d_attr + row, av, nc, vec_rows);
+        }
         if (on && p.d_bary) {
           const float4 at = load_chunk(a.attr + row, nc, vec_rows);
           db[i] += at.x * ga.x + at.y * ga.y + at.z * ga.z + at.w * ga.w;
@@ -288,12 +360,15 @@ __device__ __forceinline__ void scatter_runs(const SampleArgs& a, const PosArgs&
 // rows: contributions are summed over each run of lanes with the same
 // triangle and only the run's first lane issues the atomics (same-address
 // atomics serialize in L2).
+template <int kMode>
 __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, Batch B) {
   __shared__ int64_t s_e[kVjpBlock];
   __shared__ unsigned char s_img[kVjpBlock];
   __shared__ int s_warp[kVjpThreads / 32];
   const PosArgs& p = a.pos;
   const int lane = threadIdx.x & 31;
+  const int scale = kMode == 2 ? fixed_exponent(a) : 0;
+  float mx = 0.0f;  // kMode 1: largest magnitude this thread would add
   const int64_t total = int64_t(p.L) * B.pix_prefix[B.n];
   const int64_t q0 = int64_t(blockIdx.x) * kVjpBlock + int64_t(threadIdx.x) * kVjpPerThread;
   int img[kVjpPerThread];
@@ -402,6 +477,21 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
         }
       }
     }
+    if (kMode == 1) {
+      // First deterministic pass: a bound on what the run sums add. A run
+      // sum adds at most 32 lanes' values (each |b_i x| <= |x| max b), so
+      // 2^kRunBits times the largest per-sample value bounds it.
+      if (on) {
+        const float bm = fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2])));
+        float m = fmaxf(fixed_mag(dcl.x), fmaxf(fixed_mag(dcl.y), fixed_mag(dcl.w)));
+        if (a.d_attr_out) {
+          const float* src = a.d_attr_out + el * a.K;
+          for (int c = 0; c < a.K; ++c) m = fmaxf(m, fixed_mag(__ldg(src + c)));
+        }
+        mx = fmaxf(mx, m * fixed_mag(bm));
+      }
+      continue;
+    }
     // Runs of lanes with the same image and the same three vertex rows are
     // summed by shuffles and only each run's first lane issues the atomics
     // (measured faster than atomics from every lane even for warps of many
@@ -421,21 +511,50 @@ __global__ void __launch_bounds__(kVjpThreads) samples_bwd_kernel(SampleArgs a, 
     const unsigned span = __reduce_max_sync(0xffffffffu, unsigned(last - lane));
     float db[3];
     if (span == 0)
-      scatter_runs<0>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+      scatter_runs<0, kMode>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db, mx,
+                             scale);
     else if (span < 2)
-      scatter_runs<1>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+      scatter_runs<1, kMode>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db, mx,
+                             scale);
     else if (span < 4)
-      scatter_runs<2>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+      scatter_runs<2, kMode>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db, mx,
+                             scale);
     else if (span < 8)
-      scatter_runs<3>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+      scatter_runs<3, kMode>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db, mx,
+                             scale);
     else
-      scatter_runs<5>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db);
+      scatter_runs<5, kMode>(a, p, B, lane, last, leader, on, im, el, b, vid, V, dcl, db, mx,
+                             scale);
     if (on && p.d_bary) {
       p.d_bary[3 * el] = db[0];
       p.d_bary[3 * el + 1] = db[1];
       p.d_bary[3 * el + 2] = db[2];
     }
   }
+  if (kMode == 1) {
+    // magnitudes are >= 0 (or +inf), so their bits order as the values do
+    const unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+    if (lane == 0 && wm != 0u) atomicMax(a.fx_max, wm);
+  }
+}
+
+// Deterministic sums back to float, added to the gradients (one thread per
+// vertex).
+__global__ void __launch_bounds__(256) fixed_finalize_kernel(SampleArgs a, int64_t nv) {
+  const int64_t v = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int e = fixed_exponent(a);
+  if (e == kFixedZero || e == kFixedFloat) return;  // zeros, or float atomics took over
+  // the sum rounded to float, then scaled by 2^-e (exact unless subnormal)
+  const auto back = [e](unsigned long long q) { return ldexpf(__ll2float_rn((long long)q), -e); };
+  const unsigned long long* q = a.fx_clip + 4 * v;
+  float4 d = a.pos.d_clip[v];
+  d.x += back(q[0]);
+  d.y += back(q[1]);
+  d.w += back(q[3]);
+  a.pos.d_clip[v] = d;
+  if (a.d_attr)
+    for (int k = 0; k < a.K; ++k) a.d_attr[v * a.K + k] += back(a.fx_attr[v * a.K + k]);
 }
 
 // -------------------------------------------------------------------- splat
@@ -1642,18 +1761,45 @@ int samples_fwd_launch(const float* attributes, int K, const float* clip,
   return launch_status("interpolate + splat positions", err);
 }
 
+// Scratch of the deterministic samples VJP: the largest magnitude, then the
+// fixed-point sums of the clip and attribute gradients of every vertex the
+// images span.
+int64_t spanned_vertices(const dr_image_desc* images, int n) {
+  int64_t nv = 0;
+  for (int i = 0; i < n; ++i)
+    nv = std::max<int64_t>(nv, images[i].vertex_offset + images[i].num_vertices);
+  return nv;
+}
+
+size_t samples_fixed_bytes(const dr_image_desc* images, int n, int K) {
+  const size_t nv = size_t(spanned_vertices(images, n));
+  return 256 + ((nv * 4 * 8 + 255) & ~size_t(255)) + nv * size_t(K) * 8;
+}
+
 int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
                        const float* attributes, int K, const float* clip,
                        const int32_t* tris, const int32_t* ids, const float* z,
                        const float* bary, const float* positions,
                        const int32_t* vertex_ids, const dr_image_desc* images, int n,
                        int L, float* d_attributes, float* d_clip, float* d_bary,
+                       uint32_t flags, void* scratch, size_t scratch_bytes,
                        cudaStream_t stream, std::string& err) {
   int rc;
   if (!check_batch(L, n, images, err, rc)) return rc;
   if (K < 1 || K > DR_MAX_CHANNELS) { err = "channels must be in [1, 16]"; return DR_ERR_INVALID_ARGUMENT; }
+  if ((flags & ~DR_SAMPLES_DETERMINISTIC) != 0) {
+    err = "unknown samples backward flags";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
   if (!d_clip || (d_attr_out && !d_attributes)) {
     err = "d_clip_vertices (and d_attributes with d_attr_out) must be non-null";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  const bool det = (flags & DR_SAMPLES_DETERMINISTIC) != 0;
+  if (det && (!scratch || (reinterpret_cast<uintptr_t>(scratch) & 255) != 0 ||
+              scratch_bytes < samples_fixed_bytes(images, n, K))) {
+    err = "DR_SAMPLES_DETERMINISTIC needs a 256-byte aligned scratch of "
+          "dr_interpolate_with_positions_bwd_scratch_bytes bytes";
     return DR_ERR_INVALID_ARGUMENT;
   }
   if (!aligned16({d_positions, clip, d_clip, positions}) ||
@@ -1672,15 +1818,45 @@ int samples_bwd_launch(const float* d_attr_out, const float* d_positions,
   a.pos.d_bary = d_bary;
   a.attr = attributes; a.K = K;
   a.d_attr_out = d_attr_out; a.d_attr = d_attributes;
-  for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
-    const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
-    Batch b;
-    if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
-    const int64_t total = int64_t(L) * b.pix_prefix[cnt];
-    if (total > 0)
-      samples_bwd_kernel<<<unsigned((total + kVjpBlock - 1) / kVjpBlock), kVjpThreads, 0,
-                           stream>>>(a, b);
+  int64_t samples = 0;
+  for (int i = 0; i < n; ++i) samples += int64_t(L) * images[i].width * images[i].height;
+  const int64_t nv = spanned_vertices(images, n);
+  if (det) {
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    a.fx_max = reinterpret_cast<unsigned*>(base);
+    a.fx_clip = reinterpret_cast<unsigned long long*>(base + 256);
+    a.fx_attr = reinterpret_cast<unsigned long long*>(
+        base + 256 + ((size_t(nv) * 4 * 8 + 255) & ~size_t(255)));
+    int lc = 0;
+    while ((int64_t(1) << lc) < std::max<int64_t>(samples, 1)) ++lc;
+    a.fx_log2_count = lc;
+    if (cudaMemsetAsync(scratch, 0, samples_fixed_bytes(images, n, K), stream) != cudaSuccess) {
+      err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(cudaGetLastError());
+      return DR_ERR_CUDA;
+    }
   }
+  // Deterministic: a pass that finds the largest magnitude (no outputs), then
+  // the fixed-point pass, then the sums back to float.
+  for (int mode = det ? 1 : 0; mode <= (det ? 2 : 0); ++mode) {
+    SampleArgs am = a;
+    if (mode == 1) am.pos.d_bary = nullptr;
+    for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
+      const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
+      Batch b;
+      if (!make_batch(images + g0, cnt, L, kTX, kTY, b, err)) return DR_ERR_INVALID_ARGUMENT;
+      const int64_t total = int64_t(L) * b.pix_prefix[cnt];
+      if (total <= 0) continue;
+      const unsigned grid = unsigned((total + kVjpBlock - 1) / kVjpBlock);
+      if (mode == 0)
+        samples_bwd_kernel<0><<<grid, kVjpThreads, 0, stream>>>(am, b);
+      else if (mode == 1)
+        samples_bwd_kernel<1><<<grid, kVjpThreads, 0, stream>>>(am, b);
+      else
+        samples_bwd_kernel<2><<<grid, kVjpThreads, 0, stream>>>(am, b);
+    }
+  }
+  if (det && nv > 0)
+    fixed_finalize_kernel<<<unsigned((nv + 255) / 256), 256, 0, stream>>>(a, nv);
   return launch_status("interpolate + splat positions backward", err);
 }
 

@@ -545,13 +545,21 @@ def _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles, ids, z, wa
   d_attr = zeros[:na].view_as(attributes)
   d_clip = zeros[na_pad:].view_as(clip)
   d_bary = torch.empty_like(bary) if want_bary else None
-  with _op("samples_bwd", _groups(ctx.batch)):
-    rc = lib.dr_interpolate_with_positions_bwd(
+  deterministic = getattr(ctx, "deterministic", False)
+  flags, scratch, launches = 0, None, _groups(ctx.batch)
+  if deterministic:
+    flags = _lib.DR_SAMPLES_DETERMINISTIC
+    nbytes = lib.dr_interpolate_with_positions_bwd_scratch_bytes(
+        ctx.batch.ptr, ctx.batch.n, attributes.shape[1])
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device=clip.device)
+    launches = 2 * _groups(ctx.batch) + 1
+  with _op("samples_bwd", launches):
+    rc = lib.dr_interpolate_with_positions_bwd_ex(
         _p(d_out), _p(d_vp), _p(attributes), attributes.shape[1], _p(clip),
         _p(triangles), _p(ids), _p(z), _p(bary), _p(positions), _p(vertex_ids),
-        ctx.batch.ptr, ctx.batch.n, ctx.L, _p(d_attr), _p(d_clip), _p(d_bary),
-        _stream(clip.device))
-  _lib.check(rc, "dr_interpolate_with_positions_bwd")
+        ctx.batch.ptr, ctx.batch.n, ctx.L, flags, _p(d_attr), _p(d_clip), _p(d_bary),
+        _p(scratch), 0 if scratch is None else scratch.numel(), _stream(clip.device))
+  _lib.check(rc, "dr_interpolate_with_positions_bwd_ex")
   return d_attr, d_clip, d_bary
 
 
@@ -592,7 +600,8 @@ class _RasterSamples(torch.autograd.Function):
   gives the same bits. This trades one rasterizer pass for memory."""
 
   @staticmethod
-  def forward(ctx, attributes, clip, triangles, batch, config, workspace, recompute=False):
+  def forward(ctx, attributes, clip, triangles, batch, config, workspace, recompute=False,
+              deterministic=False):
     lib = _lib.load()
     dev = clip.device
     L = config.num_layers
@@ -612,6 +621,7 @@ class _RasterSamples(torch.autograd.Function):
           _stream(dev))
     _lib.check(rc, "dr_rasterize_batch_interpolate")
     ctx.recompute = bool(recompute)
+    ctx.deterministic = bool(deterministic)
     if recompute:
       ctx.save_for_backward(attributes, clip, triangles, z, vp)
       ctx.config, ctx.workspace = config, workspace
@@ -653,7 +663,7 @@ class _RasterSamples(torch.autograd.Function):
     d_attr, d_clip, _ = _samples_vjp(ctx, d_out, d_vp, attributes, clip, bary, triangles,
                                      ids, z, False, vp, vids)
     return (d_attr if ctx.needs_input_grad[0] else None,
-            d_clip if ctx.needs_input_grad[1] else None, None, None, None, None, None)
+            d_clip if ctx.needs_input_grad[1] else None, None, None, None, None, None, None)
 
 
 def _rerasterize(ctx, clip, triangles):
@@ -678,7 +688,7 @@ def _rerasterize(ctx, clip, triangles):
 
 
 def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, workspace,
-                                 recompute=False):
+                                 recompute=False, deterministic=False):
   """Rasterizes a packed batch and, in the same pass, interpolates
   ``attributes`` [sum V, K <= 16] (background 0) and computes the splat
   positions. Returns (attributes [L*P, K], positions [L*P, 4], ids, z, bary);
@@ -686,13 +696,15 @@ def rasterize_interpolate_packed(attributes, clip, triangles, batch, config, wor
   Positions are written for foreground samples only, as (viewport xyz,
   clip w): splat them with ``z`` so that the depth buffer marks the
   background. With ``recompute`` the VJP reruns the rasterizer instead of
-  keeping ids, barycentrics and vertex ids from the forward."""
+  keeping ids, barycentrics and vertex ids from the forward. With
+  ``deterministic`` the VJP sums the vertex gradients in fixed point, so
+  they are the same bits on every run."""
   _require_cuda(clip, triangles)
   attributes = _f32(attributes)
   if attributes.shape[1] > _lib.DR_MAX_CHANNELS:
     raise ValueError("at most %d attribute channels" % _lib.DR_MAX_CHANNELS)
   return _RasterSamples.apply(attributes, clip, triangles, batch, config, workspace,
-                              bool(recompute))
+                              bool(recompute), bool(deterministic))
 
 
 def interpolate_with_positions_packed(attributes, clip, bary, triangles, ids, z, batch,

@@ -38,7 +38,8 @@ def _shade_layers(shading_function, interpolated, num_layers, batched):
 
 
 def _render_fused(geom, attributes, shading_function, num_layers, face_culling_mode,
-                  depth_semantics, return_accum_buffers, recompute_raster=False):
+                  depth_semantics, return_accum_buffers, recompute_raster=False,
+                  deterministic_gradients=False):
   """SPLAT_OVER through the rasterizer that interpolates the attributes and
   the splat positions in its epilogue; None when the attributes exceed its
   channel limit."""
@@ -65,7 +66,7 @@ def _render_fused(geom, attributes, shading_function, num_layers, face_culling_m
                                else 0))
   interp, vp, ids, z, bary = kernels.rasterize_interpolate_packed(
       cat, geom.clip, geom.triangles_packed, geom.batch, cfg,
-      kernels.default_workspace(geom.clip.device), recompute_raster)
+      kernels.default_workspace(geom.clip.device), recompute_raster, deterministic_gradients)
   frame = rasterize.framebuffer_of(geom, num_layers, ids, z, bary)
   lead = (geom.B,) if geom.batched else ()
   interp = interp.view(*lead, num_layers, frame.height, frame.width, -1)
@@ -87,7 +88,7 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
                      compositing_mode=constants.CompositingMode.SPLAT_OVER,
                      return_accum_buffers=False, compute_diff_barys=False,
                      depth_semantics=constants.DepthSemantics.CUDA,
-                     recompute_raster=False):
+                     recompute_raster=False, deterministic_gradients=False):
   """Rendering with differentiable occlusion using rasterize-then-splat.
 
   Returns [H, W, C] ([num_layers, H, W, C] for CompositingMode.NONE), with a
@@ -98,6 +99,9 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
   beyond the reference's arguments): the single attribute is the color, as
   ``lambda a: a[key]`` gives, and background samples' attributes and color
   gradients, which nothing then reads, are not written.
+  ``deterministic_gradients`` (SPLAT_OVER; also beyond the reference): the
+  vertex and attribute gradients of the fused pass are summed in fixed
+  point, the same bits on every run.
 
   Raises:
     ValueError: if face_culling_mode is not BACK and compositing_mode is
@@ -118,7 +122,7 @@ def render_triangles(vertices, attributes: Dict[str, torch.Tensor], triangles,
       and attributes):
     fused = _render_fused(geom, attributes, shading_function, num_layers,
                           face_culling_mode, depth_semantics, return_accum_buffers,
-                          recompute_raster)
+                          recompute_raster, deterministic_gradients)
     if fused is not None:
       return fused
   frame, _ = rasterize.rasterize_geometry(geom, num_layers, face_culling_mode,

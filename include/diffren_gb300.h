@@ -329,6 +329,28 @@ int dr_interpolate_with_positions_bwd(const float* d_attributes_out,
                                       float* d_clip_vertices, float* d_barycentrics,
                                       void* stream);
 
+/* dr_interpolate_with_positions_bwd with flags. DR_SAMPLES_DETERMINISTIC:
+ * d_attributes and d_clip_vertices are summed in 64-bit fixed point (a
+ * power-of-two scale chosen from the largest value added, so that no sum
+ * can overflow) instead of with float atomics: integer sums do not depend
+ * on the order of the additions, so the gradients are the same bits on
+ * every run (and within 2^-30 of the largest addend of the exact sum). Two
+ * passes over the samples plus one over the vertices; `scratch` (256-byte
+ * aligned) holds the sums. flags = 0 is dr_interpolate_with_positions_bwd
+ * (scratch unused). */
+#define DR_SAMPLES_DETERMINISTIC 1u
+size_t dr_interpolate_with_positions_bwd_scratch_bytes(const dr_image_desc* images,
+                                                       int32_t num_images,
+                                                       int32_t num_channels);
+int dr_interpolate_with_positions_bwd_ex(
+    const float* d_attributes_out, const float* d_positions, const float* attributes,
+    int32_t num_channels, const float* clip_vertices, const int32_t* triangles,
+    const int32_t* triangle_ids, const float* z_buffer, const float* barycentrics,
+    const float* positions, const int32_t* vertex_ids, const dr_image_desc* images,
+    int32_t num_images, int32_t num_layers, uint32_t flags, float* d_attributes,
+    float* d_clip_vertices, float* d_barycentrics, void* scratch, size_t scratch_bytes,
+    void* stream);
+
 /* ---------------------------------------------------------- shaders */
 
 /* shaders.texture_map (diffren/jax/utils/shaders.py:40-65): bilinear

@@ -103,6 +103,17 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
   assert lib.dr_splat_bwd_ex(None, None, None, None, saved, 4, b.ptr, 1, 3,
                              _lib.DR_SPLAT_FOREGROUND_GRADIENTS, None, None, None) == 1
   assert b"depth buffer" in lib.dr_last_error()
+  # Samples VJP: unknown flags; the deterministic sums need their scratch.
+  assert lib.dr_interpolate_with_positions_bwd_ex(
+      None, None, None, 4, None, None, None, None, None, None, None, b.ptr, 1, 3, 2,
+      None, saved, None, None, 0, None) == 1
+  assert lib.dr_interpolate_with_positions_bwd_ex(
+      None, None, None, 4, None, None, None, None, None, None, None, b.ptr, 1, 3,
+      _lib.DR_SAMPLES_DETERMINISTIC, None, saved, None, None, 0, None) == 1
+  assert b"scratch" in lib.dr_last_error()
+  n = lib.dr_interpolate_with_positions_bwd_scratch_bytes(b.ptr, 1, 4)
+  assert n >= 256 + 3 * (4 + 4) * 8  # the header, then 3 vertices x (4 + 4) sums
+  assert lib.dr_interpolate_with_positions_bwd_scratch_bytes(b.ptr, 1, 17) == 0
   assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
                                 None) == 1
   assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1
