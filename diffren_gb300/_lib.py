@@ -103,6 +103,8 @@ SIGNATURES = {
     "dr_squared_error": (_I, [_P, _P, _L, _F, _P, _P, _P, _P]),
     "dr_vertex_normals_fwd": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "dr_vertex_normals_bwd": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P]),
+    "dr_vertex_normals_csr_fwd": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "dr_vertex_normals_csr_bwd": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "dr_splat_fwd": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
     "dr_splat_jvp": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P]),
     "dr_splat_bwd": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P]),

@@ -84,7 +84,9 @@ class BatchRenderer:
     """Area-weighted unit normals (mesh.py:22-52) of every mesh of the batch
     from packed world vertices [sum V, 3]; differentiable."""
     from . import mesh
-    return mesh.vertex_normals_packed(vertices, self.triangles, self.batch)
+    if getattr(self, "_adjacency", None) is None:
+      self._adjacency = mesh.vertex_adjacency(self.triangles, self.batch)
+    return mesh.vertex_normals_packed(vertices, self.triangles, self.batch, self._adjacency)
 
   @property
   def num_images(self):

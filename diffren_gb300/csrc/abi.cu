@@ -353,6 +353,29 @@ int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
                 err);
 }
 
+int dr_vertex_normals_csr_fwd(const float* vertices, const int32_t* triangles,
+                              const dr_image_desc* meshes, int32_t num_meshes,
+                              const int64_t* vertex_offsets, const int32_t* corners,
+                              float* face_scratch, float* accum, float* normals, void* stream) {
+  std::string err;
+  return finish(dr::normals_csr_fwd_launch(vertices, triangles, meshes, num_meshes,
+                                           vertex_offsets, corners, face_scratch, accum,
+                                           normals, as_stream(stream), err),
+                err);
+}
+
+int dr_vertex_normals_csr_bwd(const float* d_normals, const float* vertices,
+                              const int32_t* triangles, const dr_image_desc* meshes,
+                              int32_t num_meshes, const int64_t* vertex_offsets,
+                              const int32_t* corners, const float* accum, float* d_accum,
+                              float* corner_scratch, float* d_vertices, void* stream) {
+  std::string err;
+  return finish(dr::normals_csr_bwd_launch(d_normals, vertices, triangles, meshes, num_meshes,
+                                           vertex_offsets, corners, accum, d_accum,
+                                           corner_scratch, d_vertices, as_stream(stream), err),
+                err);
+}
+
 int dr_splat_positions_fwd(const float* clip_vertices, const int32_t* triangles,
                            const int32_t* triangle_ids, const float* z_buffer,
                            const float* barycentrics, const dr_image_desc* images,

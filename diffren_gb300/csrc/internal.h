@@ -137,6 +137,15 @@ int normals_bwd_launch(const float* d_normals, const float* vertices, const int3
                        const dr_image_desc* images, int n, const float* accum,
                        float* d_accum, float* d_vertices, cudaStream_t stream,
                        std::string& err);
+int normals_csr_fwd_launch(const float* vertices, const int32_t* tris,
+                           const dr_image_desc* images, int n, const int64_t* off,
+                           const int32_t* corner, float* face, float* accum, float* normals,
+                           cudaStream_t stream, std::string& err);
+int normals_csr_bwd_launch(const float* d_normals, const float* vertices, const int32_t* tris,
+                           const dr_image_desc* images, int n, const int64_t* off,
+                           const int32_t* corner, const float* accum, float* d_accum,
+                           float* corner_grad, float* d_vertices, cudaStream_t stream,
+                           std::string& err);
 
 // splat.cu
 int samples_fwd_launch(const float* attributes, int K, const float* clip,

@@ -441,6 +441,28 @@ int dr_vertex_normals_bwd(const float* d_normals, const float* vertices,
                           int32_t num_meshes, const float* accum, float* d_accum,
                           float* d_vertices, void* stream);
 
+/* The same normals without atomics, the same bits on every run, from a
+ * vertex -> corner adjacency: corner 3 g + s is slot s of global triangle g
+ * (triangles numbered in mesh order); vertex i's corners are
+ * corners[vertex_offsets[i] .. vertex_offsets[i + 1]), slot 0 ones first
+ * then slot 1 then slot 2, each in triangle order, listing no corner of a
+ * triangle with an out-of-range index (diffren_gb300.mesh builds it once
+ * per topology). Sums run in that order: the three per-slot sums in
+ * triangle order, then (s0 + s1) + s2, as three scatter-adds into zeros
+ * give. face_scratch [T, 4] and accum [V, 4] 16-byte aligned. */
+int dr_vertex_normals_csr_fwd(const float* vertices, const int32_t* triangles,
+                              const dr_image_desc* meshes, int32_t num_meshes,
+                              const int64_t* vertex_offsets, const int32_t* corners,
+                              float* face_scratch, float* accum, float* normals, void* stream);
+
+/* Its VJP: d_accum [V, 4] and corner_scratch [3 T, 4] (16-byte aligned)
+ * are scratch; d_vertices [V, 3] is accumulated into. */
+int dr_vertex_normals_csr_bwd(const float* d_normals, const float* vertices,
+                              const int32_t* triangles, const dr_image_desc* meshes,
+                              int32_t num_meshes, const int64_t* vertex_offsets,
+                              const int32_t* corners, const float* accum, float* d_accum,
+                              float* corner_scratch, float* d_vertices, void* stream);
+
 /* splat_at_pixel_centers + composite.over (splat.py:26-175,
  * composite.py:20-37): 3x3 Gaussian splats of every layer sample with the
  * per-tap surface test, normalization and back-to-front over compositing.

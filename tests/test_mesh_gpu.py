@@ -10,7 +10,7 @@ from oracle import mesh as omesh
 
 pytestmark = pytest.mark.gpu
 
-# Normals are unit vectors summed with float atomics: 1e-5 of unit length.
+# Normals are unit vectors: 1e-5 of unit length against float64.
 NORMAL_ATOL = 1e-5
 GRAD_RTOL = 1e-4
 
@@ -104,3 +104,42 @@ def test_empty_mesh(device):
   out = mesh.compute_vertex_normals(torch.tensor(v, device=device),
                                     torch.zeros(0, 3, dtype=torch.int32, device=device))
   assert torch.all(out == 0)
+
+
+def slot_sums_f32(v, t):
+  """The kernels' summation in float32: face normal cross(v1 - v0, v2 - v0)
+  with every operation rounded, per vertex the slot 0, 1 and 2 sums in
+  triangle order, then (s0 + s1) + s2 (three scatter-adds into zeros)."""
+  v = v.astype(np.float32)
+  c = v[t.astype(np.int64)]
+  e1, e2 = (c[:, 1] - c[:, 0]).astype(np.float32), (c[:, 2] - c[:, 0]).astype(np.float32)
+  n = np.stack([e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1],
+                e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2],
+                e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]], 1).astype(np.float32)
+  slots = []
+  for s in range(3):
+    acc = np.zeros_like(v)
+    np.add.at(acc, t[:, s].astype(np.int64), n)  # sequential, in triangle order
+    slots.append(acc)
+  return ((slots[0] + slots[1]) + slots[2]).astype(np.float32)
+
+
+def test_normals_are_the_same_bits_every_run_and_sum_in_triangle_order(device):
+  """The adjacency-based normals: forward and gradient repeat bit for bit,
+  and the normals equal the float32 slot-ordered sums normalized (to the
+  last bits of the reciprocal square root)."""
+  v, t = noisy_grid(40, seed=5)
+  vt = torch.tensor(v, device=device)
+  tt = torch.tensor(t, device=device)
+  g = torch.tensor(np.random.default_rng(1).standard_normal(v.shape).astype(np.float32),
+                   device=device)
+  outs = []
+  for _ in range(2):
+    x = vt.clone().requires_grad_(True)
+    out = mesh.compute_vertex_normals(x, tt)
+    (d,) = torch.autograd.grad(out, (x,), g)
+    outs.append((out.detach(), d))
+  assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+  x = slot_sums_f32(v, t).astype(np.float64)
+  ref = x / np.sqrt((x * x).sum(1, keepdims=True) + 1e-12)
+  np.testing.assert_allclose(outs[0][0].cpu().numpy(), ref, rtol=0, atol=1e-6)
