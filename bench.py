@@ -65,8 +65,8 @@ def parse():
                   help="the VJP reruns the rasterizer instead of keeping its ids, "
                        "barycentrics and vertex ids (memory-tight mode)")
   ap.add_argument("--deterministic-gradients", action="store_true",
-                  help="sum the vertex and color gradients in fixed point (same bits on "
-                       "every run)")
+                  help="sum the vertex, color and texture gradients in fixed point (same "
+                       "bits on every run)")
   ap.add_argument("--cpu-budget", type=float, default=20.0,
                   help="seconds of CPU work per reference-arm step / baseline")
   return ap.parse_args()
@@ -373,7 +373,8 @@ def run_ours(args, rank, world, device):
     c = b["cols"].detach().requires_grad_(True)
     cams = b["cams"]
     if textured:
-      out = r.render(v, {"uv": uv}, cams, lambda a: shaders.texture_map(a["uv"], c))
+      out = r.render(v, {"uv": uv}, cams, lambda a: shaders.texture_map(
+          a["uv"], c, deterministic=args.deterministic_gradients))
     elif wl.lit:
       out = r.render(v, {"rgb": c, "normals": r.vertex_normals(v), "pos": v}, cams,
                      lit_shader)

@@ -25,6 +25,7 @@ DR_MAX_SPLAT_CHANNELS = 8
 DR_MAX_BATCH_INLINE = 128
 DR_TEXTURE_PAD_ZERO = 1
 DR_TEXTURE_TEXEL_UNITS = 2
+DR_TEXTURE_DETERMINISTIC = 4
 DR_MAX_IMAGE_DIM = 32768
 DR_STATIC_SCRATCH_BYTES = 64 << 20
 DR_SQUARED_ERROR_PARTIALS = 1216
@@ -95,6 +96,8 @@ SIGNATURES = {
     "dr_splat_positions_bwd": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P]),
     "dr_texture_map_fwd": (_I, [_P, _L, _P, _I, _I, _I, _I, _P, _P]),
     "dr_texture_map_bwd": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P]),
+    "dr_texture_map_bwd_ex": (_I, [_P, _P, _L, _P, _I, _I, _I, _I, _P, _P, _P, _S, _P]),
+    "dr_texture_map_bwd_scratch_bytes": (_S, [_I, _I, _I]),
     "dr_point_light_fwd": (_I, [_P, _P, _P, _L, _I, _I, _I, _P, _P, _I, _P]),
     "dr_point_light_bwd": (_I, [_P, _I, _P, _P, _P, _L, _I, _I, _I, _P, _P, _P, _P, _I,
                                 _P]),

@@ -277,10 +277,30 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                        int32_t channels, int32_t flags, float* d_uv, float* d_texture,
                        void* stream) {
   std::string err;
+  if (flags & DR_TEXTURE_DETERMINISTIC) {
+    err = "DR_TEXTURE_DETERMINISTIC needs dr_texture_map_bwd_ex and its scratch";
+    return finish(DR_ERR_INVALID_ARGUMENT, err);
+  }
   return finish(dr::texture_bwd_launch(d_out, uv, num_points, texture, height, width,
-                                       channels, flags, d_uv, d_texture, as_stream(stream),
-                                       err),
+                                       channels, flags, d_uv, d_texture, nullptr, 0,
+                                       as_stream(stream), err),
                 err);
+}
+
+int dr_texture_map_bwd_ex(const float* d_out, const float* uv, int64_t num_points,
+                          const float* texture, int32_t height, int32_t width,
+                          int32_t channels, int32_t flags, float* d_uv, float* d_texture,
+                          void* scratch, size_t scratch_bytes, void* stream) {
+  std::string err;
+  return finish(dr::texture_bwd_launch(d_out, uv, num_points, texture, height, width,
+                                       channels, flags, d_uv, d_texture, scratch,
+                                       scratch_bytes, as_stream(stream), err),
+                err);
+}
+
+size_t dr_texture_map_bwd_scratch_bytes(int32_t height, int32_t width, int32_t channels) {
+  if (height < 1 || width < 1 || channels < 1 || channels > DR_MAX_CHANNELS) return 0;
+  return dr::texture_fixed_bytes(height, width, channels);
 }
 
 int dr_point_light_fwd(const float* diffuse, const float* normals, const float* positions,

@@ -479,6 +479,60 @@ __device__ __forceinline__ unsigned long long empty_key(int depth_mode) {
              : (unsigned long long)float_order_bits(1.0f) << 32;
 }
 
+// ---------------------------------------------------------- fixed-point sums
+// Deterministic accumulation: values are added as 64-bit integers in units of
+// 2^-e, e chosen from a bound on what is added so that no sum can overflow;
+// integer addition does not depend on order, so the sums are the same bits
+// on every run.
+constexpr int kFixedZero = -100000, kFixedFloat = -200000;
+
+// e for sums of at most 2^log2_terms values of magnitude below 2 m, m given
+// as its float bits: every sum stays below 2^62. kFixedZero when m is 0 (only
+// zeros are added), kFixedFloat when m is not finite (callers fall back to
+// float atomics, which carry the inf / NaN as the float path does).
+__device__ __forceinline__ int fixed_exponent_of(unsigned m_bits, int log2_terms) {
+  const float m = __uint_as_float(m_bits);
+  if (!(m <= 3.402823466e38f)) return kFixedFloat;
+  if (m == 0.0f) return kFixedZero;
+  return 61 - ilogbf(m) - log2_terms;
+}
+
+// round(v 2^e) in integer arithmetic: v = m 2^x with a 24-bit integer m, so
+// v 2^e = m 2^(x + e), shifted left exactly or right with rounding to
+// nearest, ties to even (|v 2^e| < 2^62 by the choice of e).
+__device__ __forceinline__ long long fixed_of(float v, int e) {
+  const unsigned u = __float_as_uint(v);
+  const int bexp = int((u >> 23) & 0xffu);
+  const unsigned m = bexp ? ((u & 0x7fffffu) | 0x800000u) : (u & 0x7fffffu);
+  const int sh = (bexp ? bexp - 150 : -149) + e;
+  long long r;
+  if (sh >= 0) {
+    r = (long long)m << sh;
+  } else if (sh < -24) {
+    r = 0;  // m 2^sh < 1/2
+  } else {
+    const int s = -sh;
+    const unsigned q = m >> s, rem = m & ((1u << s) - 1u), half = 1u << (s - 1);
+    r = (long long)(q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u));
+  }
+  return (u >> 31) ? -r : r;
+}
+
+__device__ __forceinline__ void add_fixed(unsigned long long* p, float v, int e) {
+  atomicAdd(p, (unsigned long long)fixed_of(v, e));
+}
+
+// |v| for the fixed-point scale, +inf for a non-finite v.
+__device__ __forceinline__ float fixed_mag(float v) {
+  return isfinite(v) ? fabsf(v) : __int_as_float(0x7f800000);
+}
+
+// float(q 2^-e): the integer sum rounded to float once, then scaled (exact
+// unless the result is subnormal).
+__device__ __forceinline__ float fixed_back(unsigned long long q, int e) {
+  return ldexpf(__ll2float_rn((long long)q), -e);
+}
+
 // ---------------------------------------------------------- reductions
 template <typename T>
 __device__ __forceinline__ T warp_inclusive_scan(T v) {

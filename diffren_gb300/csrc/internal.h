@@ -106,7 +106,9 @@ int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int 
                        int flags, float* out, cudaStream_t stream, std::string& err);
 int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const float* tex,
                        int H, int W, int C, int flags, float* d_uv, float* d_tex,
-                       cudaStream_t stream, std::string& err);
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream,
+                       std::string& err);
+size_t texture_fixed_bytes(int H, int W, int C);
 
 // light.cu
 int point_light_fwd_launch(const float* dif, const float* nrm, const float* pos, int64_t n,

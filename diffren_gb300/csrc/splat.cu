@@ -167,50 +167,15 @@ struct SampleArgs {
   int fx_log2_count;             // ceil(log2(bound on the additions per sum))
 };
 
-// Exponent e of the fixed-point sums (2^e units per unit) from the largest
-// magnitude added: every sum of at most 2^log2_count values stays below
-// 2^62. kFixedZero when nothing but zeros is added, kFixedFloat when a value
-// is not finite (those sums fall back to float atomics, which propagate the
-// inf / NaN as the float path does).
-constexpr int kFixedZero = -100000, kFixedFloat = -200000;
-constexpr int kRunBits = 6;  // 32 lanes per run, and margin for rounding
+// Exponent e of the fixed-point sums from the bound on what the run sums add
+// (see fixed_exponent_of): a run sum adds at most 32 lanes' values, and one
+// more bit covers their rounding.
+constexpr int kRunBits = 6;
 
 __device__ __forceinline__ int fixed_exponent(const SampleArgs& a) {
-  const float m = __uint_as_float(__ldg(a.fx_max));
-  if (!(m <= 3.402823466e38f)) return kFixedFloat;
-  if (m == 0.0f) return kFixedZero;
-  return 61 - kRunBits - ilogbf(m) - a.fx_log2_count;
+  return fixed_exponent_of(__ldg(a.fx_max), kRunBits + a.fx_log2_count);
 }
 
-// round(v 2^e) in integer arithmetic: v = m 2^x with a 24-bit integer m, so
-// v 2^e = m 2^(x + e), shifted left exactly or right with rounding to
-// nearest, ties to even (|v 2^e| < 2^62 by the choice of e).
-__device__ __forceinline__ long long fixed_of(float v, int e) {
-  const unsigned u = __float_as_uint(v);
-  const int bexp = int((u >> 23) & 0xffu);
-  const unsigned m = bexp ? ((u & 0x7fffffu) | 0x800000u) : (u & 0x7fffffu);
-  const int sh = (bexp ? bexp - 150 : -149) + e;
-  long long r;
-  if (sh >= 0) {
-    r = (long long)m << sh;
-  } else if (sh < -24) {
-    r = 0;  // m 2^sh < 1/2
-  } else {
-    const int s = -sh;
-    const unsigned q = m >> s, rem = m & ((1u << s) - 1u), half = 1u << (s - 1);
-    r = (long long)(q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u));
-  }
-  return (u >> 31) ? -r : r;
-}
-
-__device__ __forceinline__ void add_fixed(unsigned long long* p, float v, int e) {
-  atomicAdd(p, (unsigned long long)fixed_of(v, e));
-}
-
-// |v| for the fixed-point scale, +inf for a non-finite v.
-__device__ __forceinline__ float fixed_mag(float v) {
-  return isfinite(v) ? fabsf(v) : __int_as_float(0x7f800000);
-}
 
 __device__ __forceinline__ void add_chunk(float* p, float4 v, int n, bool vec) {
   if (vec) {
@@ -546,7 +511,7 @@ __global__ void __launch_bounds__(256) fixed_finalize_kernel(SampleArgs a, int64
   const int e = fixed_exponent(a);
   if (e == kFixedZero || e == kFixedFloat) return;  // zeros, or float atomics took over
   // the sum rounded to float, then scaled by 2^-e (exact unless subnormal)
-  const auto back = [e](unsigned long long q) { return ldexpf(__ll2float_rn((long long)q), -e); };
+  const auto back = [e](unsigned long long q) { return fixed_back(q, e); };
   const unsigned long long* q = a.fx_clip + 4 * v;
   float4 d = a.pos.d_clip[v];
   d.x += back(q[0]);

@@ -28,6 +28,12 @@ struct TexArgs {
   const float* d_out;
   float* d_uv;
   float* d_tex;
+  // DR_TEXTURE_DETERMINISTIC: d_tex summed in 64-bit fixed point (see
+  // fixed_exponent_of): the largest |d_out| (each texel adds w d_out with a
+  // weight w <= 1), the sums [H W C], and ceil(log2(points x 4)).
+  unsigned* fx_max;
+  unsigned long long* fx_tex;
+  int fx_log2_terms;
 };
 
 struct Axis {
@@ -266,6 +272,62 @@ __global__ void __launch_bounds__(256) texture_bwd_kernel(TexArgs a) {
   }
 }
 
+// Deterministic VJP. Pass 1: the largest |d_out| (the bound on every value a
+// texel receives). Pass 2: d_uv as texture_bwd_kernel writes it, and each
+// corner's w d_out added in fixed point. Pass 3: the sums back to float,
+// added to d_tex.
+__global__ void __launch_bounds__(256) texture_bwd_bound_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (i < a.n)
+    for (int k = 0; k < a.C; ++k) m = fmaxf(m, fixed_mag(__ldg(a.d_out + i * a.C + k)));
+  const unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+  if ((threadIdx.x & 31) == 0 && wm != 0u) atomicMax(a.fx_max, wm);
+}
+
+__global__ void __launch_bounds__(256) texture_bwd_fixed_kernel(TexArgs a) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int e = fixed_exponent_of(__ldg(a.fx_max), a.fx_log2_terms);
+  const float* g = a.d_out + i * a.C;
+  const Footprint f = footprint(a, i);
+  float du = 0.0f, dv = 0.0f;
+  for (int k = 0; k < a.C; ++k) {
+    const float gk = __ldg(g + k);
+    if (a.d_tex && gk != 0.0f && e != kFixedZero) {
+      const int64_t t[4] = {f.t00, f.t10, f.t11, f.t01};
+      const float w[4] = {f.r.fw * f.c.fw, f.r.cw * f.c.fw, f.r.cw * f.c.cw, f.r.fw * f.c.cw};
+      for (int j = 0; j < 4; ++j) {
+        if (t[j] < 0) continue;
+        const float v = gk * w[j];
+        if (e == kFixedFloat)
+          atomicAdd(a.d_tex + t[j] + k, v);  // a non-finite gradient: as the float path
+        else
+          add_fixed(a.fx_tex + t[j] + k, v, e);
+      }
+    }
+    if (a.d_uv) {
+      const float d00 = fetch(a, f.t00, k), d10 = fetch(a, f.t10, k);
+      const float d11 = fetch(a, f.t11, k), d01 = fetch(a, f.t01, k);
+      du += gk * (f.r.fw * (d01 - d00) + f.r.cw * (d11 - d10));
+      dv += gk * (f.c.fw * (d10 - d00) + f.c.cw * (d11 - d01));
+    }
+  }
+  if (a.d_uv) {
+    const bool texels = a.flags & DR_TEXTURE_TEXEL_UNITS;
+    a.d_uv[2 * i] = du * f.c.dcw * (texels ? 1.0f : __int2float_rn(a.W));
+    a.d_uv[2 * i + 1] = dv * f.r.dcw * (texels ? 1.0f : __int2float_rn(a.H));
+  }
+}
+
+__global__ void __launch_bounds__(256) texture_fixed_finalize_kernel(TexArgs a, int64_t nt) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const int e = fixed_exponent_of(__ldg(a.fx_max), a.fx_log2_terms);
+  if (e == kFixedZero || e == kFixedFloat) return;
+  a.d_tex[i] += fixed_back(a.fx_tex[i], e);
+}
+
 bool check_tex(const float* uv, int64_t n, const float* tex, int H, int W, int C,
                std::string& err) {
   if (n < 0 || H < 1 || W < 1 || C < 1 || C > DR_MAX_CHANNELS || H >= (1 << 28) ||
@@ -287,7 +349,7 @@ int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int 
   if (!check_tex(uv, n, tex, H, W, C, err)) return DR_ERR_INVALID_ARGUMENT;
   if (n == 0) return DR_OK;
   if (!out) { err = "out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
-  TexArgs a{uv, tex, H, W, C, flags, n, out, nullptr, nullptr, nullptr};
+  TexArgs a{uv, tex, H, W, C, flags, n, out, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
   const bool fast = C == 4 && !(flags & DR_TEXTURE_PAD_ZERO) &&
                     int64_t(H) * W < (int64_t(1) << 29) &&
                     (reinterpret_cast<uintptr_t>(uv) & 7) == 0 &&
@@ -299,22 +361,56 @@ int texture_fwd_launch(const float* uv, int64_t n, const float* tex, int H, int 
   return launch_status("texture map", err);
 }
 
+size_t texture_fixed_bytes(int H, int W, int C) {
+  return 256 + size_t(H) * size_t(W) * size_t(C) * 8;
+}
+
 int texture_bwd_launch(const float* d_out, const float* uv, int64_t n, const float* tex,
                        int H, int W, int C, int flags, float* d_uv, float* d_tex,
-                       cudaStream_t stream, std::string& err) {
+                       void* scratch, size_t scratch_bytes, cudaStream_t stream,
+                       std::string& err) {
   if (!check_tex(uv, n, tex, H, W, C, err)) return DR_ERR_INVALID_ARGUMENT;
+  if ((flags & ~(DR_TEXTURE_PAD_ZERO | DR_TEXTURE_TEXEL_UNITS | DR_TEXTURE_DETERMINISTIC)) != 0) {
+    err = "unknown texture flags";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
+  const bool det = (flags & DR_TEXTURE_DETERMINISTIC) != 0 && d_tex;
+  if (det && (!scratch || (reinterpret_cast<uintptr_t>(scratch) & 255) != 0 ||
+              scratch_bytes < texture_fixed_bytes(H, W, C))) {
+    err = "DR_TEXTURE_DETERMINISTIC needs a 256-byte aligned scratch of "
+          "dr_texture_map_bwd_scratch_bytes bytes";
+    return DR_ERR_INVALID_ARGUMENT;
+  }
   if (n == 0) return DR_OK;
   if (!d_out) { err = "d_out must be non-null"; return DR_ERR_INVALID_ARGUMENT; }
-  TexArgs a{uv, tex, H, W, C, flags, n, nullptr, d_out, d_uv, d_tex};
+  TexArgs a{uv, tex, H, W, C, flags, n, nullptr, d_out, d_uv, d_tex, nullptr, nullptr, 0};
+  const unsigned grid = unsigned((n + 255) / 256);
+  if (det) {
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    a.fx_max = reinterpret_cast<unsigned*>(base);
+    a.fx_tex = reinterpret_cast<unsigned long long*>(base + 256);
+    int lt = 0;
+    while ((int64_t(1) << lt) < 4 * n) ++lt;
+    a.fx_log2_terms = lt;
+    if (cudaMemsetAsync(scratch, 0, texture_fixed_bytes(H, W, C), stream) != cudaSuccess) {
+      err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(cudaGetLastError());
+      return DR_ERR_CUDA;
+    }
+    texture_bwd_bound_kernel<<<grid, 256, 0, stream>>>(a);
+    texture_bwd_fixed_kernel<<<grid, 256, 0, stream>>>(a);
+    const int64_t nt = int64_t(H) * W * C;
+    texture_fixed_finalize_kernel<<<unsigned((nt + 255) / 256), 256, 0, stream>>>(a, nt);
+    return launch_status("texture map backward", err);
+  }
   const bool fast = C == 4 && !(flags & DR_TEXTURE_PAD_ZERO) &&
                     int64_t(H) * W < (int64_t(1) << 29) &&
                     ((reinterpret_cast<uintptr_t>(uv) | reinterpret_cast<uintptr_t>(d_uv)) & 7) == 0 &&
                     ((reinterpret_cast<uintptr_t>(tex) | reinterpret_cast<uintptr_t>(d_out) |
                       reinterpret_cast<uintptr_t>(d_tex)) & 15) == 0;
   if (fast)
-    texture_bwd4_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+    texture_bwd4_kernel<<<grid, 256, 0, stream>>>(a);
   else
-    texture_bwd_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(a);
+    texture_bwd_kernel<<<grid, 256, 0, stream>>>(a);
   return launch_status("texture map backward", err);
 }
 

@@ -43,12 +43,21 @@ class _Resample(torch.autograd.Function):
     d_img = torch.zeros_like(image) if ctx.needs_input_grad[1] else None
     if d_pts is None and d_img is None:
       return None, None, None
-    with kernels._op("texture_bwd", 1):
-      rc = lib.dr_texture_map_bwd(kernels._p(d_out.contiguous()), kernels._p(points),
-                                  points.shape[0], kernels._p(image), H, W, C, ctx.flags,
-                                  kernels._p(d_pts), kernels._p(d_img),
-                                  kernels._stream(points.device))
-    _lib.check(rc, "dr_texture_map_bwd")
+    flags, scratch, launches = ctx.flags, None, 1
+    if flags & _lib.DR_TEXTURE_DETERMINISTIC:
+      if d_img is None:
+        flags &= ~_lib.DR_TEXTURE_DETERMINISTIC  # d_uv is per point: nothing to sum
+      else:
+        scratch = torch.empty(lib.dr_texture_map_bwd_scratch_bytes(H, W, C),
+                              dtype=torch.uint8, device=points.device)
+        launches = 3
+    with kernels._op("texture_bwd", launches):
+      rc = lib.dr_texture_map_bwd_ex(kernels._p(d_out.contiguous()), kernels._p(points),
+                                     points.shape[0], kernels._p(image), H, W, C, flags,
+                                     kernels._p(d_pts), kernels._p(d_img), kernels._p(scratch),
+                                     0 if scratch is None else scratch.numel(),
+                                     kernels._stream(points.device))
+    _lib.check(rc, "dr_texture_map_bwd_ex")
     return d_pts, d_img, None
 
 
@@ -64,24 +73,29 @@ def _resample(points, image, flags):
   return out.view(*points.shape[:-1], image.shape[-1])
 
 
-def texture_map(uv_image, texture_image):
+def _det(deterministic):
+  return _lib.DR_TEXTURE_DETERMINISTIC if deterministic else 0
+
+
+def texture_map(uv_image, texture_image, deterministic=False):
   """Bilinear texture lookup with edge clamping (shaders.py:40-65).
 
   uv_image [..., 2] with u along the texture's width and v along its height
   (range [0, 1]); texture_image [H, W, C]. Returns [..., C]. Differentiable
-  w.r.t. both.
+  w.r.t. both. ``deterministic`` (beyond the reference's arguments): the
+  texture gradient is summed in fixed point, the same bits on every run.
   """
-  return _resample(uv_image, texture_image, 0)
+  return _resample(uv_image, texture_image, _det(deterministic))
 
 
-def bilinear_resample(image, locations, pad_mode="constant"):
+def bilinear_resample(image, locations, pad_mode="constant", deterministic=False):
   """image.bilinear_resample (image.py:21-118) for 'HWC' order: samples
   image [H, W, C] at locations [..., 2] in texel units, 'xy' order, samples
   at half-integer coordinates; pad_mode 'constant' (zeros) or 'edge'."""
   if pad_mode not in ("constant", "edge"):
     raise ValueError("Unsupported padding mode: %s" % pad_mode)
   flags = _lib.DR_TEXTURE_TEXEL_UNITS | (_lib.DR_TEXTURE_PAD_ZERO if pad_mode == "constant"
-                                         else 0)
+                                         else 0) | _det(deterministic)
   return _resample(locations, image, flags)
 
 

@@ -362,6 +362,10 @@ int dr_interpolate_with_positions_bwd_ex(
  * (image.bilinear_resample's locations). */
 #define DR_TEXTURE_PAD_ZERO 1
 #define DR_TEXTURE_TEXEL_UNITS 2
+/* dr_texture_map_bwd_ex only: d_texture summed in 64-bit fixed point (the
+ * scale from the largest |d_out|) instead of with float atomics, the same
+ * bits on every run. */
+#define DR_TEXTURE_DETERMINISTIC 4
 int dr_texture_map_fwd(const float* uv, int64_t num_points, const float* texture,
                        int32_t height, int32_t width, int32_t channels, int32_t flags,
                        float* out, void* stream);
@@ -372,6 +376,15 @@ int dr_texture_map_bwd(const float* d_out, const float* uv, int64_t num_points,
                        const float* texture, int32_t height, int32_t width,
                        int32_t channels, int32_t flags, float* d_uv, float* d_texture,
                        void* stream);
+
+/* dr_texture_map_bwd with a scratch buffer (256-byte aligned, of
+ * dr_texture_map_bwd_scratch_bytes bytes), which DR_TEXTURE_DETERMINISTIC
+ * needs for its fixed-point sums. */
+size_t dr_texture_map_bwd_scratch_bytes(int32_t height, int32_t width, int32_t channels);
+int dr_texture_map_bwd_ex(const float* d_out, const float* uv, int64_t num_points,
+                          const float* texture, int32_t height, int32_t width,
+                          int32_t channels, int32_t flags, float* d_uv, float* d_texture,
+                          void* scratch, size_t scratch_bytes, void* stream);
 
 /* shaders.point_light (shaders.py:100-173): ambient + diffuse + Blinn-Phong
  * specular lighting with quadratic distance attenuation, per sample. */

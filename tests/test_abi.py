@@ -97,7 +97,7 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
   assert lib.dr_splat_bwd(None, None, None, None, None, 4, b.ptr, 1, 3, None, None,
                           None) == 1
   # Unknown splat flags; foreground-only color gradients need the depth buffer.
-  saved = ctypes.c_void_p(256)
+  saved = fake = ctypes.c_void_p(256)
   assert lib.dr_splat_bwd_ex(None, None, None, None, saved, 4, b.ptr, 1, 3, 2, None, None,
                              None) == 1
   assert lib.dr_splat_bwd_ex(None, None, None, None, saved, 4, b.ptr, 1, 3,
@@ -114,6 +114,16 @@ def test_entry_points_reject_bad_arguments_without_gpu_work():
   n = lib.dr_interpolate_with_positions_bwd_scratch_bytes(b.ptr, 1, 4)
   assert n >= 256 + 3 * (4 + 4) * 8  # the header, then 3 vertices x (4 + 4) sums
   assert lib.dr_interpolate_with_positions_bwd_scratch_bytes(b.ptr, 1, 17) == 0
+  # Texture VJP: the deterministic sums need the _ex entry point and its scratch.
+  assert lib.dr_texture_map_bwd(fake, fake, 10, fake, 4, 4, 4, _lib.DR_TEXTURE_DETERMINISTIC,
+                                fake, fake, None) == 1
+  assert lib.dr_texture_map_bwd_ex(fake, fake, 10, fake, 4, 4, 4,
+                                   _lib.DR_TEXTURE_DETERMINISTIC, fake, fake, None, 0,
+                                   None) == 1
+  assert b"scratch" in lib.dr_last_error()
+  assert lib.dr_texture_map_bwd_ex(fake, fake, 10, fake, 4, 4, 4, 8, fake, fake, None, 0,
+                                   None) == 1
+  assert lib.dr_texture_map_bwd_scratch_bytes(4, 4, 4) == 256 + 4 * 4 * 4 * 8
   assert lib.dr_interpolate_fwd(None, 17, None, None, None, None, None, b.ptr, 1, 3, None,
                                 None) == 1
   assert lib.dr_transform_vertices(None, None, 5, b.ptr, 1, None, None) == 1

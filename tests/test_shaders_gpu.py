@@ -209,3 +209,30 @@ def test_point_light_kernel_matches_oracle(kw, packed, device):
   ours = (torch.cat([x for x in ours], 1) if not packed else ours[0]).cpu().numpy()
   for k in range(3):
     assert_grad_close(ours[:, 3 * k:3 * k + 3], refg[k].numpy())
+
+
+@pytest.mark.parametrize("C", [4, 3])
+def test_deterministic_texture_gradient_repeats_bit_for_bit(C, device):
+  """texture_map(..., deterministic=True): the texture gradient summed in
+  fixed point is the same bits on two runs and within 1e-6 of the
+  float-atomic sum's largest magnitude; the uv gradient and the image are
+  unchanged."""
+  rng = np.random.default_rng(C)
+  tex = torch.tensor(rng.uniform(-1, 1, (37, 53, C)).astype(np.float32), device=device)
+  uv = torch.tensor(rng.uniform(-0.1, 1.1, (20000, 2)).astype(np.float32), device=device)
+  g = torch.tensor(rng.standard_normal((20000, C)).astype(np.float32), device=device)
+
+  def run(det):
+    t = tex.clone().requires_grad_(True)
+    u = uv.clone().requires_grad_(True)
+    out = shaders.texture_map(u, t, deterministic=det)
+    dt, du = torch.autograd.grad(out, (t, u), g)
+    return out.detach(), dt, du
+
+  o1, t1, u1 = run(True)
+  o2, t2, u2 = run(True)
+  o0, t0, u0 = run(False)
+  assert torch.equal(o1, o2) and torch.equal(o1, o0)
+  assert torch.equal(t1, t2) and torch.equal(u1, u2)
+  assert float((t1 - t0).abs().max()) <= 1e-6 * float(t0.abs().max())
+  torch.testing.assert_close(u1, u0, rtol=1e-6, atol=1e-6)
