@@ -439,3 +439,55 @@ def test_deterministic_gradients_repeat_bit_for_bit(recompute, device):
   assert torch.equal(gv1, gv2) and torch.equal(gc1, gc2)
   for a, b in ((gv1, gv0), (gc1, gc0)):
     assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
+
+
+def test_batches_over_the_inline_limit_match_per_image(device):
+  """131 images (more than DR_MAX_BATCH_INLINE = 128): every kernel splits
+  its launches into groups of images and the splat runs one block per tile
+  instead of the tile list. Each image still equals its own
+  render_triangles call bit for bit, gradients within 1e-4, and the
+  deterministic mode (fixed-point sums spanning both groups) repeats its
+  bits."""
+  n = _lib.DR_MAX_BATCH_INLINE + 3
+  meshes = [workloads.icosphere_workload(2, seed=i) if i % 2 == 0 else
+            workloads.soup_workload(40, seed=i, mu=-1.5, sigma=0.4) for i in range(n)]
+  rng = np.random.default_rng(11)
+  sizes = [(int(rng.integers(8, 41)), int(rng.integers(8, 41))) for _ in range(n)]
+  eyes = workloads.sphere_eyes(n, seed=13, radius=2.6)
+  cams = [workloads.camera_matrix(e, w, h) for e, (w, h) in zip(eyes, sizes)]
+  cam = torch.tensor(np.stack(cams), device=device)
+  voff = np.cumsum([0] + [len(m.vertices) for m in meshes])
+
+  def run(det):
+    r = batch_lib.BatchRenderer([m.triangles for m in meshes], [len(m.vertices) for m in meshes],
+                                sizes, num_layers=3, device=device, deterministic_gradients=det)
+    v = torch.tensor(np.concatenate([m.vertices for m in meshes]), device=device,
+                     requires_grad=True)
+    c = torch.tensor(np.concatenate([m.colors for m in meshes]), device=device,
+                     requires_grad=True)
+    out = r.render(v, {"rgba": rgba(c)}, cam, rgba_shader)
+    g = torch.tensor(np.random.default_rng(5).standard_normal(tuple(out.shape))
+                     .astype(np.float32), device=device)
+    gv, gc = torch.autograd.grad(out, (v, c), g)
+    return r, out.detach(), g, gv, gc
+
+  r, out, g, gv, gc = run(False)
+  _, out1, _, gv1, gc1 = run(True)
+  _, out2, _, gv2, gc2 = run(True)
+  assert torch.equal(out1, out) and torch.equal(out2, out)
+  assert torch.equal(gv1, gv2) and torch.equal(gc1, gc2)
+  for a, b in ((gv1, gv), (gc1, gc)):
+    assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
+  imgs, gimgs = r.images(out), r.images(g)
+  assert sum(int((im[..., 3] > 0).any()) for im in imgs) > n // 2
+  for i in range(n):
+    m, (w, h) = meshes[i], sizes[i]
+    vi = torch.tensor(m.vertices, device=device, requires_grad=True)
+    ci = torch.tensor(m.colors, device=device, requires_grad=True)
+    oi = render.render_triangles(vi, {"rgba": rgba(ci)}, torch.tensor(m.triangles, device=device),
+                                 cam[i], w, h, rgba_shader, num_layers=3)
+    torch.testing.assert_close(imgs[i], oi, rtol=0, atol=0)
+    gvi, gci = torch.autograd.grad(oi, (vi, ci), gimgs[i])
+    sl = slice(int(voff[i]), int(voff[i + 1]))
+    torch.testing.assert_close(gv[sl], gvi, rtol=1e-4, atol=1e-4 * float(gvi.abs().max()) + 1e-12)
+    torch.testing.assert_close(gc[sl], gci, rtol=1e-4, atol=1e-4 * float(gci.abs().max()) + 1e-12)
