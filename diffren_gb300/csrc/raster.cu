@@ -60,12 +60,14 @@ struct RasterArgs {
   int4* bbox;  // {left, right, bottom, top}; empty when culled
   int32_t* tile_count;  // triangles inside one tile (their slots come from here)
   int32_t* tile_multi;  // triangles spanning 2..large_tiles tiles
-  int32_t* tile_fill;   // bin slots taken by the multi-tile triangles
+  int32_t* tile_fill;   // bin slots taken by the multi-tile triangles; after
+                        // binning, the tiles in the fine rasterizer's order
   int32_t* tile_first;  // exclusive scan of tile_count + tile_multi, total_tiles + 1
   int32_t* bins;        // global triangle indices grouped by tile
   int32_t* large_count;  // per image
   int32_t* large_list;   // per image, at tri_start[image]
-  uint32_t* counters;    // [0] work queue head, [1] error flags
+  uint32_t* counters;    // [0] work queue head, [1] error flags, [2, 8) tiles
+                         // per cost class, [8, 14) their fill counts
   int32_t* ids;
   float* z;
   float* bary;
@@ -83,7 +85,7 @@ size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 Layout make_layout(int64_t tris, int64_t tiles, int images, int large_tiles) {
   Layout l;
   size_t o = 0;
-  l.counters = o; o = align_up(o + 64);  // [0] queue head, [1] error flags
+  l.counters = o; o = align_up(o + 64);  // queue head, error flags, tile order counts
   l.tile_count = o; o = align_up(o + 4 * tiles);
   l.tile_multi = o; o = align_up(o + 4 * tiles);
   l.tile_fill = o; o = align_up(o + 4 * tiles);
@@ -289,6 +291,57 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(RasterArgs a, Batch B)
     }
 }
 
+// Tile order of the fine rasterizer: the most expensive tiles first, so that
+// no block is left with a heavy tile while the others have run out of work
+// (the per-tile cost spans three orders of magnitude in ragged batches). The
+// cost of a tile is its triangle count (binned plus the image's large ones),
+// in six classes, heaviest first; inside a class tiles keep roughly their
+// index order (block by block), which keeps an image's tiles together in L2.
+// The order does not change any output: tiles are independent.
+constexpr int kCostClasses = 6;
+
+__device__ __forceinline__ int cost_class(const RasterArgs& a, int tile, int img) {
+  const int c = a.tile_first[tile + 1] - a.tile_first[tile] + a.large_count[img];
+  return c >= 512 ? 0 : c >= 128 ? 1 : c >= 32 ? 2 : c >= 8 ? 3 : c >= 2 ? 4 : 5;
+}
+
+// Tiles per cost class (counters[2 + class]), one shared-memory histogram
+// per block.
+__global__ void __launch_bounds__(256) tile_cost_kernel(RasterArgs a, Batch B) {
+  __shared__ int h[kCostClasses];
+  if (threadIdx.x < kCostClasses) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.total_tiles) atomicAdd(&h[cost_class(a, i, find_segment(B.tile_start, B.n, i))], 1);
+  __syncthreads();
+  if (threadIdx.x < kCostClasses && h[threadIdx.x])
+    atomicAdd(&a.counters[2 + threadIdx.x], unsigned(h[threadIdx.x]));
+}
+
+// Writes every tile index to its place in the order (tile_fill, free once
+// the bins are filled): class c starts after the tiles of classes < c, and
+// each block takes a run of its classes' slots (counters[8 + class]).
+__global__ void __launch_bounds__(256) tile_order_kernel(RasterArgs a, Batch B) {
+  __shared__ int h[kCostClasses], base[kCostClasses];
+  if (threadIdx.x < kCostClasses) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0, rank = 0;
+  if (i < a.total_tiles) {
+    c = cost_class(a, i, find_segment(B.tile_start, B.n, i));
+    rank = atomicAdd(&h[c], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < kCostClasses) {
+    int start = 0;
+    for (int k = 0; k < int(threadIdx.x); ++k) start += int(a.counters[2 + k]);
+    const int n = h[threadIdx.x];
+    base[threadIdx.x] = start + (n ? int(atomicAdd(&a.counters[8 + threadIdx.x], unsigned(n))) : 0);
+  }
+  __syncthreads();
+  if (i < a.total_tiles) a.tile_fill[base[c] + rank] = i;
+}
+
 // Per chunk of up to kThreads triangles overlapping the tile, compacted to
 // those with at least one candidate pixel (slot = rank among them).
 struct FineSmem {
@@ -319,7 +372,7 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 }
 
 // Persistent fine rasterizer. Each block takes (image, tile) items from a
-// global queue, keeps the tile's L x TW x TH packed keys in shared memory,
+// global queue (heaviest tiles first, in tile_order_kernel's order), keeps the tile's L x TW x TH packed keys in shared memory,
 // and spreads the (triangle, pixel) candidates of each chunk of the tile's
 // triangles evenly over its threads (block prefix scan + binary search), so
 // large and small triangles cost the same per pixel.
@@ -417,8 +470,8 @@ __global__ void __launch_bounds__(kThreads, 8) fine_raster_kernel(RasterArgs a,
   for (;;) {
     if (threadIdx.x == 0) s_item = int(atomicAdd(&a.counters[0], 1u));
     __syncthreads();
-    const int item = s_item;
-    if (item >= a.total_tiles) break;
+    if (s_item >= a.total_tiles) break;
+    const int item = a.tile_fill[s_item];  // heaviest tiles first
     const int img = find_segment(B.tile_start, B.n, item);
     const int local = item - B.tile_start[img];
     const int W = B.width[img], H = B.height[img];
@@ -883,6 +936,11 @@ int raster_launch(const float* vertices, const int32_t* triangles,
     if (tris > 0) {
       const unsigned grid = unsigned((tris + 255) / 256);
       bin_scatter_kernel<<<grid, 256, 0, stream>>>(a, b);
+    }
+    if (tiles > 0) {
+      const unsigned grid = unsigned((tiles + 255) / 256);
+      tile_cost_kernel<<<grid, 256, 0, stream>>>(a, b);
+      tile_order_kernel<<<grid, 256, 0, stream>>>(a, b);
     }
     const int blocks = std::max(1, std::min(tiles, sms * per_sm));
     fine[variant]<<<blocks, kThreads, smem, stream>>>(a, b);

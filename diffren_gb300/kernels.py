@@ -239,7 +239,7 @@ def rasterize_packed(clip, triangles, batch, config, workspace=None, out=None):
     ids, z, bary = out
   need = raster_workspace_bytes(batch, config)
   ws = (workspace or default_workspace(dev)).get(need)
-  with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
+  with torch.cuda.device(dev), _op("raster", 6 * _groups(batch)):
     rc = lib.dr_rasterize_batch(_p(clip), _p(triangles), batch.ptr, batch.n,
                                 ctypes.byref(config), _p(ids), _p(z), _p(bary),
                                 _p(ws), ws.numel(), _stream(dev))
@@ -614,7 +614,7 @@ class _RasterSamples(torch.autograd.Function):
     vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
     vids = None if recompute else torch.empty(n, 3, dtype=torch.int32, device=dev)
     ws = workspace.get(raster_workspace_bytes(batch, config))
-    with torch.cuda.device(dev), _op("raster", 4 * _groups(batch)):
+    with torch.cuda.device(dev), _op("raster", 6 * _groups(batch)):
       rc = lib.dr_rasterize_batch_interpolate(
           _p(clip), _p(triangles), batch.ptr, batch.n, ctypes.byref(config), _p(ids), _p(z),
           _p(bary), _p(attributes), K, _p(out), _p(vp), _p(vids), _p(ws), ws.numel(),
@@ -678,7 +678,7 @@ def _rerasterize(ctx, clip, triangles):
   vp = torch.empty(n, 4, dtype=torch.float32, device=dev)
   vids = torch.empty(n, 3, dtype=torch.int32, device=dev)
   ws = ctx.workspace.get(raster_workspace_bytes(ctx.batch, ctx.config))
-  with torch.cuda.device(dev), _op("raster_recompute", 4 * _groups(ctx.batch)):
+  with torch.cuda.device(dev), _op("raster_recompute", 6 * _groups(ctx.batch)):
     rc = lib.dr_rasterize_batch_interpolate(
         _p(clip), _p(triangles), ctx.batch.ptr, ctx.batch.n, ctypes.byref(ctx.config),
         _p(ids), _p(z), _p(bary), None, 0, None, _p(vp), _p(vids), _p(ws), ws.numel(),
