@@ -372,10 +372,11 @@ __host__ __device__ inline size_t fine_smem_bytes(int L, int TW, int TH) {
 }
 
 // Persistent fine rasterizer. Each block takes (image, tile) items from a
-// global queue (heaviest tiles first, in tile_order_kernel's order), keeps the tile's L x TW x TH packed keys in shared memory,
-// and spreads the (triangle, pixel) candidates of each chunk of the tile's
-// triangles evenly over its threads (block prefix scan + binary search), so
-// large and small triangles cost the same per pixel.
+// global queue (heaviest tiles first, in tile_order_kernel's order), keeps
+// the tile's L x TW x TH packed keys in shared memory, and spreads the
+// (triangle, pixel) candidates of each chunk of the tile's triangles evenly
+// over its threads (block prefix scan + binary search), so large and small
+// triangles cost the same per pixel.
 // Fused interpolation of one layer sample o with triangle `id` and the
 // barycentrics just written: the splat position of a foreground sample
 // (splat.py:207-221) with its clip w, its three vertex indices when
