@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -52,6 +54,54 @@ inline bool make_batch(const dr_image_desc* images, int n, int L, int TW, int TH
     err = "batch too large: triangles and tiles must each be < 2^31";
     return false;
   }
+  return true;
+}
+
+constexpr int kMaxDevices = 64;
+
+// Host-side cache of one kernel's launch attributes on each device: the
+// dynamic shared-memory limit raised so far, and SMs x resident blocks per
+// SM for one shared-memory size. Host threads may launch concurrently, so
+// every use holds the lock; the limit only grows.
+struct LaunchCache {
+  std::mutex mu;
+  size_t raised[kMaxDevices] = {};
+  size_t occ_smem[kMaxDevices] = {};
+  int sms[kMaxDevices] = {};
+  int per_sm[kMaxDevices] = {};
+};
+
+// Raises kern's dynamic shared-memory limit on the current device to smem
+// when needed (`too_big` is the error when the device cannot), and returns
+// the SM count and the resident blocks per SM of `threads`-thread blocks
+// with smem bytes (at least 1).
+template <typename K>
+bool prepare_launch(LaunchCache& c, K kern, int threads, size_t smem, int& sms, int& per_sm,
+                    const char* too_big, std::string& err) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    err = "no usable CUDA device";
+    return false;
+  }
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (smem > 48 * 1024 && smem > c.raised[dev]) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
+        cudaSuccess) {
+      err = too_big;
+      return false;
+    }
+    c.raised[dev] = smem;
+  }
+  if (c.per_sm[dev] == 0 || c.occ_smem[dev] != smem) {
+    int n = 0, p = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, kern, threads, smem);
+    c.sms[dev] = std::max(1, n);
+    c.per_sm[dev] = std::max(1, p);
+    c.occ_smem[dev] = smem;
+  }
+  sms = c.sms[dev];
+  per_sm = c.per_sm[dev];
   return true;
 }
 

@@ -754,33 +754,13 @@ __global__ void depth_codec_selftest_kernel(unsigned long long* out) {
 }
 
 // Raises the fine rasterizer's dynamic shared-memory limit and computes its
-// persistent grid (resident blocks per SM x SMs), once per instantiation
-// and shared-memory size (host-side attributes only).
+// persistent grid (resident blocks per SM x SMs) on the current device.
 template <bool kFused, int LT>
 bool prepare_fine(size_t smem, int& sms, int& per_sm, std::string& err) {
-  static size_t smem_set = 0, occ_smem = 0;
-  static int s_sms = 0, s_per_sm = 0;
-  if (smem > 48 * 1024 && smem > smem_set) {
-    if (cudaFuncSetAttribute(fine_raster_kernel<kFused, LT>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem)) != cudaSuccess) {
-      err = "tile and layer count need more shared memory than the device has";
-      return false;
-    }
-    smem_set = smem;
-  }
-  if (occ_smem != smem) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&s_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per_sm, fine_raster_kernel<kFused, LT>,
-                                                  kThreads, smem);
-    if (s_per_sm < 1) s_per_sm = 1;
-    occ_smem = smem;
-  }
-  sms = s_sms;
-  per_sm = s_per_sm;
-  return true;
+  static LaunchCache cache;
+  return prepare_launch(cache, fine_raster_kernel<kFused, LT>, kThreads, smem, sms, per_sm,
+                        "tile and layer count need more shared memory than the device has",
+                        err);
 }
 
 int resolve_tile(int v) { return v > 0 ? v : kDefaultTile; }

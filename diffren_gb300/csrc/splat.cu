@@ -1534,34 +1534,6 @@ TileList tile_list(const SplatArgs& a, int tiles) {
   return t;
 }
 
-// Resident blocks per SM x SMs of a persistent kernel (host-side queries,
-// once per kernel and shared-memory size).
-template <typename K>
-int persistent_grid(K kern, size_t smem, size_t& cached_smem, int& cached_grid) {
-  if (cached_smem != smem || cached_grid == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTX * kTY, smem);
-    cached_grid = std::max(1, sms * std::max(1, per_sm));
-    cached_smem = smem;
-  }
-  return cached_grid;
-}
-
-template <typename K>
-bool reserve_smem(K kern, size_t smem, size_t& reserved, std::string& err) {
-  if (smem > 48 * 1024 && smem > reserved) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem)) != cudaSuccess) {
-      err = "layers x channels need more shared memory than the device has";
-      return false;
-    }
-    reserved = smem;
-  }
-  return true;
-}
-
 // With saved accumulators and a depth buffer (the training path) a call is
 // split: a light kernel classifies the tiles (forward) or zeros the
 // gradients of the empty ones (backward), and the heavy kernel runs
@@ -1573,13 +1545,14 @@ int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
   const size_t smem = bwd ? bwd_smem(a.L, C) : fwd_smem(a.L, C);
   auto kern = bwd ? splat_bwd_kernel<C, LT> : splat_fwd_kernel<C, LT>;
   auto list_kern = bwd ? splat_bwd_list_kernel<C, LT> : splat_fwd_list_kernel<C, LT>;
-  // Raise the dynamic shared-memory limit once per kernel and size (host-side
-  // attribute only; later calls skip it).
-  static size_t reserved[2] = {0, 0}, reserved_list[2] = {0, 0};
-  static size_t grid_smem[2] = {0, 0};
-  static int grid_blocks[2] = {0, 0};
-  if (!reserve_smem(kern, smem, reserved[bwd], err) ||
-      !reserve_smem(list_kern, smem, reserved_list[bwd], err))
+  // Dynamic shared-memory limits (host-side attributes, raised once per
+  // device and size) and the persistent grid of the list kernel.
+  static LaunchCache cache[2], list_cache[2];
+  const char* too_big = "layers x channels need more shared memory than the device has";
+  int sms = 0, per_sm = 0, list_sms = 0, list_per_sm = 0;
+  if (!prepare_launch(cache[bwd], kern, kTX * kTY, smem, sms, per_sm, too_big, err) ||
+      !prepare_launch(list_cache[bwd], list_kern, kTX * kTY, smem, list_sms, list_per_sm,
+                      too_big, err))
     return DR_ERR_INVALID_ARGUMENT;
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
     const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
@@ -1594,8 +1567,7 @@ int run_splat(bool bwd, SplatArgs a, const dr_image_desc* images, int n,
       continue;
     }
     const TileList t = tile_list<C>(a, tiles);
-    const int grid = std::min(tiles, persistent_grid(list_kern, smem, grid_smem[bwd],
-                                                     grid_blocks[bwd]));
+    const int grid = std::min(tiles, list_sms * list_per_sm);
     const unsigned light = unsigned((tiles + 7) / 8);
     if (!bwd) {
       if (cudaMemsetAsync(t.count, 0, kListHeader, stream) != cudaSuccess) {
@@ -1621,15 +1593,11 @@ int run_splat_jvp(const SplatArgs& a, const float4* d_vp, const float* d_colors,
                   float* d_image, const dr_image_desc* images, int n, cudaStream_t stream,
                   std::string& err) {
   const size_t smem = jvp_smem(a.L, C);
-  static size_t reserved = 0;
-  if (smem > 48 * 1024 && smem > reserved) {
-    if (cudaFuncSetAttribute(splat_jvp_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem)) != cudaSuccess) {
-      err = "layers x channels need more shared memory than the device has";
-      return DR_ERR_INVALID_ARGUMENT;
-    }
-    reserved = smem;
-  }
+  static LaunchCache cache;
+  int sms = 0, per_sm = 0;
+  if (!prepare_launch(cache, splat_jvp_kernel<C>, kTX * kTY, smem, sms, per_sm,
+                      "layers x channels need more shared memory than the device has", err))
+    return DR_ERR_INVALID_ARGUMENT;
   for (int g0 = 0; g0 < n; g0 += DR_MAX_BATCH_INLINE) {
     const int cnt = std::min(n - g0, DR_MAX_BATCH_INLINE);
     Batch b;
